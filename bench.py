@@ -1,0 +1,516 @@
+#!/usr/bin/env python
+"""Assembly throughput on one GB300: elements/s and HBM-roofline fraction.
+
+Headline workload: FP64 linear-elasticity stiffness (bilform_lin_elastic,
+DeforModelRed3D) of a seeded T10 block, 60 x 60 x 60 cells split into six
+tetrahedra each (1,296,000 elements, 1,771,561 nodes, 3 DOFs per node,
+451,604,169 nonzeros), 4-point tet rule, isotropic E = 210e9, nu = 0.3.
+A step is one full assembly into the device-resident CSR matrix.
+
+Also measured (the `workloads` key): the H20 40^3 elasticity stiffness with
+per-element (E, nu), FP64 vs mixed precision, and the H8 20^3 diffusion
+stiffness.
+
+  python bench.py [--steps K] [--warmup W] [--gpus N] [--impl reference]
+
+Under torchrun every rank assembles its own replica (weak scaling, no
+collective on the data path); rank 0 prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+T10_N = 60          # cells per side of the headline mesh
+H20_N = 40
+H8_N = 20
+CPU_SAMPLE_N = 24   # T10 cells per side of the timed CPU-baseline sample
+REF_SAMPLE_N = 12   # per-worker T10 sample of the reference arm
+
+
+# ---------------------------------------------------------------------------
+def env_rank():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return p.get("hbm_gbs"), "measured"
+    except (OSError, ValueError):
+        return 6800.0, "fallback"
+
+
+def traffic_record():
+    """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def algorithmic_bytes(nelem, nne, nnodes, nnz, ndof, s_coef):
+    """Pattern resident, values written once: connectivity (int32), FP64
+    coordinates, coefficients, FP64 values written, int32 column indices read,
+    int32 row pointers."""
+    return nelem * nne * 4 + nnodes * 3 * 8 + nelem * s_coef + nnz * 8 + nnz * 4 + (ndof + 1) * 4
+
+
+# ---------------------------------------------------------------------------
+# CPU oracle baseline (the only place bench.py runs oracle/)
+def _oracle_t10_sample(n, reps):
+    import __graft_entry__ as entry
+    ft = entry.load_package()
+    O = entry.load_oracle()
+    fens, fes = ft.t10_elastic_mesh(n=n)
+    femm = ft.IntegDomain(fes, ft.TetRule(4))
+    npts, Ns, dN, w, pc = femm.integrationdata()
+    u = ft.numberdofs(ft.NodalField(np.zeros((fens.count(), 3))))
+    D = ft.isotropic_D(210e9, 0.3)
+    times = []
+    for _ in range(reps):
+        t = time.perf_counter()
+        O.bilform(O.LIN_ELASTIC, O.T10, fes.conn, fens.xyz, u.dofnums, u.nalldofs(), pc, w, D)
+        times.append(time.perf_counter() - t)
+    return fes.count(), times
+
+
+_WORKER = {}
+
+
+def _ref_worker_init(n):
+    import __graft_entry__ as entry
+    ft = entry.load_package()
+    O = entry.load_oracle()
+    fens, fes = ft.t10_elastic_mesh(n=n)
+    dom = ft.IntegDomain(fes, ft.TetRule(4))
+    npts, Ns, dN, w, pc = dom.integrationdata()
+    u = ft.numberdofs(ft.NodalField(np.zeros((fens.count(), 3))))
+    _WORKER.update(O=O, fes=fes, fens=fens, u=u, pc=pc, w=w, D=ft.isotropic_D(210e9, 0.3))
+
+
+def _ref_worker_step(_):
+    W = _WORKER
+    O = W["O"]
+    t = time.perf_counter()
+    O.bilform(O.LIN_ELASTIC, O.T10, W["fes"].conn, W["fens"].xyz, W["u"].dofnums,
+              W["u"].nalldofs(), W["pc"], W["w"], W["D"])
+    return W["fes"].count(), time.perf_counter() - t
+
+
+def run_reference(args):
+    """The reference algorithm (serial C restatement) on every host core: each
+    step, every worker assembles its own T10 block; elements/s summed."""
+    rank, world, _ = env_rank()
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores, initializer=_ref_worker_init, initargs=(REF_SAMPLE_N,)) as pool:
+        for _ in range(args.warmup):
+            pool.map(_ref_worker_step, range(cores))
+        t0 = time.perf_counter()
+        elems = 0
+        for _ in range(args.steps):
+            elems += sum(e for e, _ in pool.map(_ref_worker_step, range(cores)))
+        dt = time.perf_counter() - t0
+    value = elems / dt
+    sample = (f"{cores} processes, each assembling a T10 {REF_SAMPLE_N}^3 block "
+              f"({6 * REF_SAMPLE_N ** 3} elements) per step with the serial C restatement")
+    out = {
+        "impl": "reference", "metric": "elements/s", "value": value, "unit": "elements/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded T10 blocks)",
+        "config": {"workload": f"T10 {args.t10_n}^3 linear elasticity (bilform_lin_elastic), FP64",
+                   "sample": f"T10 {REF_SAMPLE_N}^3 blocks, one per host core per step"},
+        "cpu_baseline": {"value": value, "unit": "elements/s", "cores": cores, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "elements/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+# ---------------------------------------------------------------------------
+class Lib:
+    """Thin access to the C ABI for timing."""
+
+    def __init__(self, ft, device):
+        from importlib import import_module
+        self.nat = import_module(ft.__name__ + "._native")
+        self.L = self.nat.load()
+        self.ctx = self.nat.context(device)
+        s = C.c_void_p()
+        self.nat.check(self.L.fegpu_context_stream(self.ctx, C.byref(s)))
+        self.stream = s.value
+        self.nat.check(self.L.fegpu_context_timing(self.ctx, 1))
+
+    def stats(self, reset=True):
+        ms = C.c_double()
+        n = C.c_int64()
+        self.nat.check(self.L.fegpu_context_kernel_stats(self.ctx, C.byref(ms), C.byref(n),
+                                                         int(reset)))
+        return ms.value, n.value
+
+
+def pinned(torch, shape, dtype):
+    t = torch.empty(int(np.prod(shape)), dtype=dtype, pin_memory=True)
+    return t.numpy().reshape(shape)
+
+
+def time_steps(torch, stream, fn, steps, warmup, flush=None, dist=None):
+    """Device time of `steps` calls of fn on the library stream (CUDA events),
+    barrier + synchronize on both sides; max over ranks."""
+    for _ in range(warmup):
+        fn()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    if flush is None:
+        ev[0].record(stream)
+        for _ in range(steps):
+            fn()
+        ev[1].record(stream)
+        torch.cuda.synchronize()
+        ms = ev[0].elapsed_time(ev[1])
+    else:  # per-step events with an L2 flush in between
+        ms = 0.0
+        for _ in range(steps):
+            flush()
+            torch.cuda.synchronize()
+            ev[0].record(stream)
+            fn()
+            ev[1].record(stream)
+            torch.cuda.synchronize()
+            ms += ev[0].elapsed_time(ev[1])
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms
+
+
+def fp64_peak_tflops(torch):
+    """Measured FP64 GEMM throughput (torch.matmul, float64, 8192^3)."""
+    a = torch.randn(8192, 8192, dtype=torch.float64, device="cuda")
+    b = torch.randn(8192, 8192, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    ev[0].record()
+    torch.matmul(a, b)
+    ev[1].record()
+    torch.cuda.synchronize()
+    ms = ev[0].elapsed_time(ev[1])
+    del a, b
+    return 2 * 8192 ** 3 / (ms * 1e-3) / 1e12
+
+
+def elastic_flops_per_element(nne, npts):
+    """FP64 operations per element of the elasticity kernel as written: per point
+    J (2 nne 9), det + inverse (~60), gradients (nne 3 5), weighting (3 nne);
+    per node-pair block the Gram sums (18 npts), the Lame map (33) and the
+    scatter adds (9 per block written)."""
+    per_qp = 2 * nne * 9 + 60 + nne * 3 * 5 + 3 * nne
+    nblk = nne * (nne + 1) // 2
+    return npts * per_qp + nblk * (18 * npts + 33) + 9 * nne * nne
+
+
+def run_ours(args):
+    import torch
+    rank, world, local = env_rank()
+    dist = None
+    if world > 1:
+        import torch.distributed as tdist
+        tdist.init_process_group("nccl")
+        dist = tdist
+    torch.cuda.set_device(local)
+    import __graft_entry__ as entry
+    ft = entry.load_package()
+    lib = Lib(ft, local)
+    stream = torch.cuda.ExternalStream(lib.stream, device=local)
+
+    # ---------------- headline: T10 60^3, FP64
+    t0 = time.perf_counter()
+    fens, fes = ft.t10_elastic_mesh(n=args.t10_n)
+    mesh_s = time.perf_counter() - t0
+    geom = ft.NodalField(fens.xyz)
+    u = ft.numberdofs(ft.NodalField(np.zeros((fens.count(), 3))))
+    D = ft.isotropic_D(210e9, 0.3)
+    femm = ft.FEMMBase(ft.IntegDomain(fes, ft.TetRule(4)), device=local)
+    asm = ft.SysmatAssemblerGPU(result="device", device=local)
+    t0 = time.perf_counter()
+    femm.set_geometry(geom)
+    dm = femm.dofmap(u)
+    K = ft.bilform_lin_elastic(femm, asm, geom, u, ft.DeforModelRed3D, ft.DataCache(D))
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+    ncol = femm.colors()[1]
+    cD = np.ascontiguousarray(D.ravel())
+    coef = lib.nat.Coef(lib.nat.COEF_CONST, 36, cD.ctypes.data)
+
+    def step():
+        lib.nat.check(lib.L.fegpu_bilform_lin_elastic(K.h, C.byref(coef), lib.nat.FP64))
+
+    lib.stats(reset=True)
+    with ClockSampler(local) as clk:
+        ms = time_steps(torch, stream, step, args.steps, args.warmup, dist=dist)
+    kms, launches = lib.stats(reset=True)
+    # the warm-up steps are in the counters too
+    nsteps_counted = args.steps + args.warmup
+    kernel_ms_step = kms / nsteps_counted
+    launches_timed = launches // nsteps_counted * args.steps
+    E, N, nnz, ndof = fes.count(), fens.count(), dm.nnz, dm.ndof
+    ms_step = ms / args.steps
+    value = world * E / (ms_step * 1e-3)
+    B = algorithmic_bytes(E, 10, N, nnz, ndof, 0)
+    peak, peak_src = measured_peaks()
+    achieved = B / (kernel_ms_step * 1e-3) / 1e9
+    traffic = traffic_record().get("t10_fp64")
+    fp64_peak = fp64_peak_tflops(torch)
+    flops = elastic_flops_per_element(10, 4) * E
+
+    # ---------------- end to end through the C ABI with host buffers
+    xyz_h = pinned(torch, (3, N), torch.float64)  # column-major nnodes x 3
+    xyz_h[:] = fens.xyz.T
+    vals_h = pinned(torch, (nnz,), torch.float64)
+
+    def e2e_step():
+        lib.nat.check(lib.L.fegpu_femm_set_geometry(femm._h, 3, xyz_h.ctypes.data))
+        lib.nat.check(lib.L.fegpu_bilform_lin_elastic(K.h, C.byref(coef), lib.nat.FP64))
+        lib.nat.check(lib.L.fegpu_matrix_copy_values(K.h, vals_h.ctypes.data))
+
+    for _ in range(args.warmup):
+        e2e_step()
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    if dist is not None:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * E * args.steps / e2e_s
+    lib.stats(reset=True)
+    del K, asm
+    femm = None
+    torch.cuda.empty_cache()
+
+    workloads = {}
+    if not args.headline_only:
+        workloads["h20_40_elasticity"] = bench_h20(ft, torch, lib, stream, args, local, dist)
+        workloads["h8_20_diffusion"] = bench_h8(ft, torch, lib, stream, args, local, dist)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        ne, times = _oracle_t10_sample(CPU_SAMPLE_N, 3)
+        cpu = {"value": ne / min(times), "unit": "elements/s", "cores": 1, "kind": "port",
+               "sample": f"T10 {CPU_SAMPLE_N}^3 block ({ne} elements), bilform_lin_elastic + "
+                         "makematrix! in the serial C restatement, best of 3"}
+    if rank != 0:
+        return
+    out = {
+        "metric": "elements/s", "value": value, "unit": "elements/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": f"synthetic: seeded T10 {args.t10_n}^3 block, interior vertices jittered +-0.15h",
+        "config": {"workload": f"T10 {args.t10_n}^3 linear elasticity (bilform_lin_elastic), FP64",
+                   "elements": E, "nodes": N, "dofs": ndof, "nnz": nnz, "colours": ncol,
+                   "l2": "working set larger than L2 (CSR values alone 3.6 GB); no flush",
+                   "parallelism": f"replicas x{world}"},
+        "nnz_per_s": world * nnz / (ms_step * 1e-3),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
+                     "algorithmic_bytes_per_assembly": B,
+                     "kernel": "k_form<T10, ELAST_ISO, double, 3>, one launch per colour",
+                     "kernel_ms_per_assembly": kernel_ms_step},
+        "fp64_pipe": {"achieved_tflops": flops / (kernel_ms_step * 1e-3) / 1e12,
+                      "peak_tflops": fp64_peak, "frac": flops / (kernel_ms_step * 1e-3) / 1e12 /
+                      fp64_peak, "peak_source": "measured: torch.matmul float64 8192^3",
+                      "flops_per_assembly": flops},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": "elements/s", "h2d_bytes_per_step": N * 3 * 8,
+                "d2h_bytes_per_step": nnz * 8,
+                "path": "fegpu_femm_set_geometry (pinned host coordinates) + "
+                        "fegpu_bilform_lin_elastic + fegpu_matrix_copy_values (pinned host)"},
+        "gpu_launches": launches_timed,
+        "clocks": clk.summary(),
+        "setup_s": {"mesh": mesh_s, "pattern_colouring_first_assembly": setup_s},
+        "workloads": workloads,
+    }
+    print(json.dumps(out), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def bench_h20(ft, torch, lib, stream, args, local, dist):
+    fens, fes, flagged = ft.h20_elastic_mesh(n=H20_N)
+    rng = np.random.default_rng(4)
+    E = rng.lognormal(np.log(70e9), 0.5, fes.count())
+    nu = rng.uniform(0.2, 0.35, fes.count())
+    cf = ft.IsotropicElementwise(E, nu)
+    geom = ft.NodalField(fens.xyz)
+    u = ft.numberdofs(ft.NodalField(np.zeros((fens.count(), 3))))
+    femm = ft.FEMMBase(ft.IntegDomain(fes, ft.GaussRule(3, 3)), device=local)
+    res = {"elements": fes.count(), "distorted_elements": int(len(flagged))}
+    mats = {}
+    for prec in ("fp64", "mixed"):
+        asm = ft.SysmatAssemblerGPU(precision=prec, result="device", device=local)
+        K = ft.bilform_lin_elastic(femm, asm, geom, u, ft.DeforModelRed3D, cf)
+        lame = np.ascontiguousarray(cf.lame)
+        coef = lib.nat.Coef(lib.nat.COEF_ISO_LAME, 2, lame.ctypes.data)
+        code = lib.nat.FP64 if prec == "fp64" else lib.nat.MIXED
+
+        def step(K=K, coef=coef, code=code):
+            lib.nat.check(lib.L.fegpu_bilform_lin_elastic(K.h, C.byref(coef), code))
+
+        lib.stats(reset=True)
+        ms = time_steps(torch, stream, step, args.steps, args.warmup, dist=dist)
+        kms, _ = lib.stats(reset=True)
+        ms_step = ms / args.steps
+        dm = K.dm
+        B = algorithmic_bytes(fes.count(), 20, fens.count(), dm.nnz, dm.ndof, 16)
+        peak, _ = measured_peaks()
+        kstep = kms / (args.steps + args.warmup)
+        res[prec] = {"elements_per_s": fes.count() / (ms_step * 1e-3), "ms_per_step": ms_step,
+                     "kernel_ms": kstep, "hbm_frac": B / (kstep * 1e-3) / 1e9 / peak,
+                     "algorithmic_bytes": B}
+        mats[prec] = K
+    v64 = mats["fp64"].values()
+    v32 = mats["mixed"].values()
+    x = np.random.default_rng(3).uniform(-1, 1, mats["fp64"].shape[0])
+    y64 = mats["fp64"].spmv(x)
+    y32 = mats["mixed"].spmv(x)
+    res["mixed_vs_fp64"] = {
+        "max_abs_over_max": float(np.abs(v32 - v64).max() / np.abs(v64).max()),
+        "rel_Kx": float(np.linalg.norm(y32 - y64) / np.linalg.norm(y64)),
+    }
+    res["speedup_mixed_over_fp64"] = res["mixed"]["elements_per_s"] / res["fp64"]["elements_per_s"]
+    return res
+
+
+def bench_h8(ft, torch, lib, stream, args, local, dist):
+    fens, fes = ft.h8_diffusion_mesh(n=H8_N)
+    geom = ft.NodalField(fens.xyz)
+    u = ft.numberdofs(ft.NodalField(np.zeros((fens.count(), 1))))
+    femm = ft.FEMMBase(ft.IntegDomain(fes, ft.GaussRule(3, 2)), device=local)
+    asm = ft.SysmatAssemblerGPU(result="device", device=local)
+    K = ft.bilform_diffusion(femm, asm, geom, u, ft.DataCache(1.0))
+    c1 = np.array([1.0])
+    coef = lib.nat.Coef(lib.nat.COEF_CONST, 1, c1.ctypes.data)
+    scratch = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+
+    def flush():
+        scratch.zero_()
+
+    def step():
+        lib.nat.check(lib.L.fegpu_bilform_diffusion(K.h, C.byref(coef), lib.nat.FP64))
+
+    ms = time_steps(torch, stream, step, args.steps, args.warmup, flush=flush, dist=dist)
+    lib.stats(reset=True)
+    ms_step = ms / args.steps
+    return {"elements": fes.count(), "nnz": K.dm.nnz, "ms_per_step": ms_step,
+            "elements_per_s": fes.count() / (ms_step * 1e-3),
+            "l2": "flushed between steps (256 MB write)"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--headline-only", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--t10-n", type=int, default=T10_N,
+                    help="cells per side of the headline T10 block (60 = the benchmark size)")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

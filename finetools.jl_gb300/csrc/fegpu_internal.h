@@ -1,0 +1,186 @@
+// Internal declarations of libfegpu: handle layouts, kernel argument blocks and
+// the launchers that api.cu dispatches to.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/fegpu.h"
+
+namespace fegpu {
+
+// ---- error plumbing --------------------------------------------------------
+void set_error(const std::string &msg);
+struct Error {
+  int code;
+  std::string msg;
+};
+#define FEGPU_CUDA(call)                                                        \
+  do {                                                                          \
+    cudaError_t e_ = (call);                                                    \
+    if (e_ != cudaSuccess)                                                      \
+      throw ::fegpu::Error{e_ == cudaErrorMemoryAllocation ? FEGPU_ERR_MEMORY   \
+                                                           : FEGPU_ERR_CUDA,    \
+                           std::string(#call) + ": " + cudaGetErrorString(e_)}; \
+  } while (0)
+#define FEGPU_REQUIRE(cond, msg)                              \
+  do {                                                        \
+    if (!(cond)) throw ::fegpu::Error{FEGPU_ERR_ARG, (msg)}; \
+  } while (0)
+
+// ---- device buffer ----------------------------------------------------------
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  void alloc(size_t n) {
+    if (n <= bytes && p) return;
+    release();
+    if (n == 0) n = 16;
+    FEGPU_CUDA(cudaMalloc(&p, n));
+    bytes = n;
+  }
+  template <typename T>
+  T *as() const { return static_cast<T *>(p); }
+};
+
+// ---- element facts ---------------------------------------------------------
+inline int nodes_per_elem(int et) {
+  switch (et) {
+    case FEGPU_Q4: return 4;
+    case FEGPU_H8: return 8;
+    case FEGPU_H20: return 20;
+    case FEGPU_T4: return 4;
+    case FEGPU_T10: return 10;
+  }
+  return 0;
+}
+inline int manif_dim(int et) { return et == FEGPU_Q4 ? 2 : 3; }
+inline int max_qp(int et) {
+  switch (et) {
+    case FEGPU_Q4: return 16;
+    case FEGPU_H8: return 27;
+    case FEGPU_H20: return 27;
+    case FEGPU_T4: return 5;
+    case FEGPU_T10: return 5;
+  }
+  return 0;
+}
+
+}  // namespace fegpu
+
+// ---- handles (opaque to callers) -------------------------------------------
+struct fegpu_context {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  fegpu::DevBuf scratch;   // CUB temporaries, compaction buffers
+  fegpu::DevBuf scratch2;
+  bool timing = false;      // events around the element-kernel launches
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double kernel_ms = 0.0;   // accumulated element-kernel time
+  int64_t launches = 0;     // kernels launched by the library
+};
+
+struct fegpu_femm {
+  fegpu_context *ctx = nullptr;
+  int etype = 0, nne = 0, mdim = 0, npts = 0, sdim = 0;
+  int64_t nelem = 0, nnodes = 0;
+  double otherdim = 1.0;
+  std::vector<int64_t> colors;         // element order, 1-based
+  std::vector<int64_t> color_offsets;  // sorted-element ranges per colour
+  fegpu::DevBuf conn_orig;             // int32 nelem x nne, 0-based, element order
+  fegpu::DevBuf conn;                  // int32 nelem x nne, colour-sorted
+  fegpu::DevBuf perm;                  // int32 sorted position -> element
+  fegpu::DevBuf tab;                   // double: N[q][k], dN[q][k][m], w[q]
+  fegpu::DevBuf xyz;                   // double [nnodes][4]
+  bool has_geometry = false;
+};
+
+struct fegpu_dofmap {
+  fegpu_femm *femm = nullptr;
+  int ndn = 0;
+  int64_t ndof = 0, nnz = 0;
+  int maxdeg = 0;
+  bool contiguous = true;   // every node's DOFs are consecutive numbers
+  fegpu::DevBuf dof;        // int32 [nnodes][ndn], 0-based
+  fegpu::DevBuf rowptr;     // int64 [ndof + 1]
+  fegpu::DevBuf colind;     // int32 [nnz]
+  fegpu::DevBuf pos;        // uint16 [nelem][nne][nne], colour-sorted elements
+  fegpu::DevBuf colperm;    // int32 per node block, only if !contiguous
+  fegpu::DevBuf cpoff;      // int64 [nnodes], only if !contiguous
+};
+
+struct fegpu_matrix {
+  fegpu_dofmap *dm = nullptr;
+  fegpu::DevBuf val;  // double [nnz]
+};
+
+namespace fegpu {
+
+// ---- element-kernel forms ----------------------------------------------------
+enum Form {
+  F_DIFF_ISO = 0,   // scalar conductivity
+  F_DIFF_GEN = 1,   // mdim x mdim conductivity
+  F_ELAST_ISO = 2,  // lambda, mu
+  F_ELAST_GEN = 3,  // 6x6 D
+  F_DOT = 4,        // N N' c
+  F_LIN = 5,        // N f  (vector)
+};
+
+// Kernel argument block (passed by value; < 1 KB).
+struct KArgs {
+  const int32_t *conn;     // colour-sorted nelem x nne
+  const double *xyz;       // [nnodes][4]
+  const double *tab;       // N, dN, w tables
+  const uint16_t *pos;     // colour-sorted nelem x nne x nne
+  const int32_t *dof;      // [nnodes][ndn]
+  const int64_t *rowptr;   // CSR rows
+  const int32_t *colperm;  // null when the numbering is node-contiguous
+  const int64_t *cpoff;
+  double *val;             // CSR values, or the dense vector for F_LIN
+  const double *coef;      // device coefficient array (colour-sorted) or null
+  int coef_kind;           // FEGPU_COEF_*
+  int ncomp;
+  double cconst[36];       // constant coefficient
+  double cab[9], cba[9], cdiag[9];  // bilform_dot block coefficients
+  int npts, sdim, te;
+  int measure_m;           // manifold dimension of the measure (dot, linform)
+  double otherdim;
+  double distort_tol;      // mixed path: det_min/det_max below -> FP64 geometry
+  int64_t e0, e1;          // colour range of sorted elements
+  int *status;             // device status word (0 = ok)
+};
+
+// Launch one colour of one form.  Returns the number of kernel launches made.
+int launch_form(int etype, int form, int precision, int ndn, const KArgs &a,
+                int num_sms, cudaStream_t s);
+size_t form_smem_bytes(int etype, int form, int precision, int npts, int te);
+int choose_tile(int etype, int form, int precision, int npts);
+
+// ---- host colouring (element_coloring!) ---------------------------------------
+int64_t greedy_element_coloring(int64_t nelem, int nne, const int32_t *conn0,
+                                int64_t nnodes, std::vector<int64_t> &colors);
+
+// ---- pattern build on the device ------------------------------------------------
+void build_pattern(fegpu_dofmap *dm, const std::vector<int32_t> &hdof);
+
+// ---- matrix utilities -----------------------------------------------------------
+void spmv(const fegpu_dofmap *dm, const double *val, const double *x, double *y,
+          cudaStream_t s);
+int64_t count_nonzeros(fegpu_context *ctx, const fegpu_dofmap *dm, const double *val);
+void copy_csc(fegpu_context *ctx, const fegpu_dofmap *dm, const double *val,
+              int drop_zeros, int64_t *colptr, int64_t *rowval, double *nzval);
+
+}  // namespace fegpu

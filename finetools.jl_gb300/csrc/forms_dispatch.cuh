@@ -1,0 +1,51 @@
+// Per-element-type dispatch over (form, precision, DOFs per node).  One
+// translation unit per element type instantiates it (forms_<type>.cu) so the
+// build compiles them in parallel.
+#pragma once
+
+#include "elements.cuh"
+
+namespace fegpu {
+
+template <int ET>
+int launch_form_et(int form, int precision, int ndn, const KArgs &a, int sms, cudaStream_t s) {
+  constexpr bool SOLID = ElemT<ET>::MDIM == 3;
+  const bool mixed = precision == FEGPU_MIXED;
+  switch (form) {
+    case F_DIFF_ISO:
+      return mixed ? launch_one<ET, F_DIFF_ISO, float, 1>(a, sms, s)
+                   : launch_one<ET, F_DIFF_ISO, double, 1>(a, sms, s);
+    case F_DIFF_GEN:
+      return mixed ? launch_one<ET, F_DIFF_GEN, float, 1>(a, sms, s)
+                   : launch_one<ET, F_DIFF_GEN, double, 1>(a, sms, s);
+    case F_ELAST_ISO:
+      if constexpr (SOLID)
+        return mixed ? launch_one<ET, F_ELAST_ISO, float, 3>(a, sms, s)
+                     : launch_one<ET, F_ELAST_ISO, double, 3>(a, sms, s);
+      break;
+    case F_ELAST_GEN:
+      if constexpr (SOLID)
+        return mixed ? launch_one<ET, F_ELAST_GEN, float, 3>(a, sms, s)
+                     : launch_one<ET, F_ELAST_GEN, double, 3>(a, sms, s);
+      break;
+    case F_DOT:
+      if (ndn == 1) return launch_one<ET, F_DOT, double, 1>(a, sms, s);
+      if (ndn == 2) return launch_one<ET, F_DOT, double, 2>(a, sms, s);
+      if (ndn == 3) return launch_one<ET, F_DOT, double, 3>(a, sms, s);
+      break;
+    case F_LIN:
+      if (ndn == 1) return launch_one<ET, F_LIN, double, 1>(a, sms, s);
+      if (ndn == 2) return launch_one<ET, F_LIN, double, 2>(a, sms, s);
+      if (ndn == 3) return launch_one<ET, F_LIN, double, 3>(a, sms, s);
+      break;
+  }
+  throw Error{FEGPU_ERR_ARG, "form not available for this element type / DOF count"};
+}
+
+int launch_form_q4(int, int, int, const KArgs &, int, cudaStream_t);
+int launch_form_h8(int, int, int, const KArgs &, int, cudaStream_t);
+int launch_form_h20(int, int, int, const KArgs &, int, cudaStream_t);
+int launch_form_t4(int, int, int, const KArgs &, int, cudaStream_t);
+int launch_form_t10(int, int, int, const KArgs &, int, cudaStream_t);
+
+}  // namespace fegpu

@@ -1,0 +1,8 @@
+// Element kernels for FEGPU_Q4 (all forms, both precisions).
+#include "forms_dispatch.cuh"
+
+namespace fegpu {
+int launch_form_q4(int form, int precision, int ndn, const KArgs &a, int sms, cudaStream_t s) {
+  return launch_form_et<FEGPU_Q4>(form, precision, ndn, a, sms, s);
+}
+}  // namespace fegpu

@@ -1,0 +1,182 @@
+/*
+ * fegpu.h -- C ABI of the GB300 finite-element assembly library (libfegpu.so).
+ *
+ * The library replaces the element-by-element form evaluation and the sparse
+ * COO->CSC assembly of FinEtools.jl (v8.2.11) for one GPU.  Every entry point
+ * is plain C: opaque handles, host pointers and sizes; no CUDA or torch types.
+ * A Julia caller reaches it through `ccall`; Python through ctypes.
+ *
+ * Conventions (identical to the Julia objects the reference passes around):
+ *   - node and DOF numbers are 1-based;
+ *   - connectivity is nelem x nne, row-major (Vector{NTuple{nne,Int}});
+ *   - nodal values (geometry) and DOF numbers are nnodes x k, column-major
+ *     (NodalField.values / NodalField.dofnums);
+ *   - results are SparseMatrixCSC{Float64,Int64} arrays (colptr, rowval,
+ *     nzval), 1-based.
+ * Every function returns FEGPU_OK (0) or a nonzero status; the message of the
+ * most recent failure on the calling thread is fegpu_last_error().
+ * Handles are externally synchronised: one thread at a time per context.
+ */
+#ifndef FEGPU_H
+#define FEGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define FEGPU_OK 0
+#define FEGPU_ERR_ARG 1      /* invalid argument (sizes, numbers, kinds)     */
+#define FEGPU_ERR_CUDA 2     /* CUDA runtime failure                          */
+#define FEGPU_ERR_MEMORY 3   /* device allocation failed                      */
+#define FEGPU_ERR_STATE 4    /* handle used out of order                      */
+#define FEGPU_ERR_DEVICE 5   /* a device-side check failed (bad data)         */
+
+/* element types (src/FESetModule.jl: FESetQ4 711, FESetH8 953, FESetH20
+ * 1028, FESetT4 1342, FESetT10 1393) */
+#define FEGPU_Q4 0
+#define FEGPU_H8 1
+#define FEGPU_H20 2
+#define FEGPU_T4 3
+#define FEGPU_T10 4
+
+/* coefficient kinds: the DataCache forms a caller can hand over
+ * (src/DataCacheModule.jl:65-112) */
+#define FEGPU_COEF_CONST 0        /* one value set, as DataCache(data)        */
+#define FEGPU_COEF_PER_ELEMENT 1  /* nelem x ncomp, row-major (per feid)      */
+#define FEGPU_COEF_PER_QP 2       /* nelem x npts x ncomp (per feid, qpid)    */
+#define FEGPU_COEF_ISO_LAME 3     /* nelem x 2 (lambda, mu): per-element      */
+                                  /* isotropic elasticity                     */
+
+/* arithmetic of the element kernels */
+#define FEGPU_FP64 0   /* plain FP64 throughout                               */
+#define FEGPU_MIXED 1  /* FP32 bulk (FP64 geometry for distorted elements,    */
+                       /* FP64 global accumulation)                           */
+
+typedef struct fegpu_context fegpu_context;
+typedef struct fegpu_femm fegpu_femm;
+typedef struct fegpu_dofmap fegpu_dofmap;
+typedef struct fegpu_matrix fegpu_matrix;
+typedef struct fegpu_vector_assembler fegpu_vector_assembler;
+typedef struct fegpu_assembler fegpu_assembler;
+
+typedef struct {
+  int kind;            /* FEGPU_COEF_*                                       */
+  int ncomp;           /* values per element / quadrature point              */
+  const double *data;  /* host pointer                                       */
+} fegpu_coef;
+
+/* Message of the last failed call on this thread ("" if none). */
+const char *fegpu_last_error(void);
+
+/* ---- context: one GPU, one CUDA stream ---------------------------------- */
+int fegpu_context_create(int device, fegpu_context **out);
+int fegpu_context_destroy(fegpu_context *ctx);
+int fegpu_context_synchronize(fegpu_context *ctx);
+/* The context's CUDA stream (a cudaStream_t), for callers that order their
+ * own work or record events around library calls.  No reference counterpart:
+ * interoperability only. */
+int fegpu_context_stream(fegpu_context *ctx, void **stream);
+/* Kernel accounting (no reference counterpart): with timing enabled, every
+ * form records CUDA events around its element-kernel launches on the
+ * context's stream; kernel_stats returns the accumulated element-kernel time
+ * (ms) and the number of kernels the library launched, and resets them when
+ * reset != 0. */
+int fegpu_context_timing(fegpu_context *ctx, int enable);
+int fegpu_context_kernel_stats(fegpu_context *ctx, double *kernel_ms, int64_t *launches,
+                               int reset);
+
+/* ---- FEMMBase: element set + integration data, resident on the device ---
+ * Replaces FEMMBase(IntegDomain(fes, rule[, otherdimension]))
+ * (src/FEMMBaseModule.jl:72-84, src/IntegDomainModule.jl:43-143) together
+ * with integrationdata() (src/IntegDomainModule.jl:610-648): the caller
+ * passes the basis-function tables the reference computes at the quadrature
+ * points (Ns: npts x nne, gradNparams: npts x nne x mdim, row-major; w: npts)
+ * so that the kernels use exactly the caller's rule.  Builds the node ->
+ * element map and the greedy element colouring of element_coloring!
+ * (src/FENodeToFEMapModule.jl:44-74, src/MeshModificationModule.jl:1287-1365). */
+int fegpu_femm_create(fegpu_context *ctx, int etype, int64_t nelem,
+                      const int64_t *conn, int64_t nnodes, int npts,
+                      const double *Ns, const double *gradNparams,
+                      const double *w, double otherdimension,
+                      fegpu_femm **out);
+int fegpu_femm_destroy(fegpu_femm *femm);
+/* geometry NodalField values (nnodes x sdim, column-major), uploaded and kept
+ * resident; call again to move the nodes (re-assembly on new coordinates). */
+int fegpu_femm_set_geometry(fegpu_femm *femm, int sdim, const double *xyz);
+/* element colours (1-based, element order) and their count. */
+int fegpu_femm_colors(fegpu_femm *femm, int64_t *colors, int64_t *ncolors);
+
+/* ---- DOF map: NodalField dofnums -> CSR pattern built on the device ------
+ * Replaces the structure half of makematrix! (the sparse() call,
+ * src/AssemblyModule.jl:319, 567) and connectionmatrix
+ * (src/FEMMBaseModule.jl:490-510).  dofnums: nnodes x ndn column-major,
+ * 1-based, every DOF numbered (src/FieldModule.jl:328-377); nalldofs as
+ * returned by nalldofs(u).  Reports the structural nnz. */
+int fegpu_dofmap_create(fegpu_femm *femm, int ndn, const int64_t *dofnums,
+                        int64_t nalldofs, fegpu_dofmap **out, int64_t *nnz);
+int fegpu_dofmap_destroy(fegpu_dofmap *dm);
+/* structural pattern as CSC (symmetric, so CSC == CSR), 1-based. */
+int fegpu_dofmap_copy_pattern(fegpu_dofmap *dm, int64_t *colptr, int64_t *rowval);
+
+/* ---- global matrix resident on the device --------------------------------
+ * The device-side counterpart of SysmatAssemblerSparseSymm / Sparse
+ * (src/AssemblyModule.jl:88-583): values live in the dofmap's CSR pattern. */
+int fegpu_matrix_create(fegpu_dofmap *dm, fegpu_matrix **out);
+int fegpu_matrix_destroy(fegpu_matrix *K);
+
+/* The forms.  Each one zeroes K and assembles every element into it with the
+ * deterministic colour-ordered scatter.
+ *   bilform_diffusion: src/FEMMBaseModule.jl:1462-1545 (scalar ncomp = 1 ->
+ *     _bilform_diffusion_iso, mdim x mdim -> _bilform_diffusion_general);
+ *   bilform_lin_elastic(DeforModelRed3D): src/FEMMBaseModule.jl:1774-1824
+ *     (ncomp = 36: 6x6 D in Voigt order xx,yy,zz,xy,xz,yz, row-major; or
+ *     FEGPU_COEF_ISO_LAME);
+ *   bilform_dot: src/FEMMBaseModule.jl:1335-1376 (ncomp = ndn*ndn; m is the
+ *     manifold dimension of the measure, as in Jacobianmdim).
+ * symmetric = 1 reproduces SysmatAssemblerSparseSymm (the element matrix's
+ * lower triangle by local index, mirrored), 0 reproduces SysmatAssemblerSparse. */
+int fegpu_bilform_diffusion(fegpu_matrix *K, const fegpu_coef *cf, int precision);
+int fegpu_bilform_lin_elastic(fegpu_matrix *K, const fegpu_coef *cf, int precision);
+int fegpu_bilform_dot(fegpu_matrix *K, const fegpu_coef *cf, int m, int symmetric,
+                      int precision);
+
+/* linform_dot / distribloads (src/FEMMBaseModule.jl:1207-1297) into a dense
+ * vector, SysvecAssembler semantics (src/AssemblyModule.jl:853-917).
+ * f: ncomp = ndn.  F: nalldofs doubles (host). */
+int fegpu_linform_dot(fegpu_dofmap *dm, const fegpu_coef *f, int m, double *F);
+
+/* makematrix! output.  drop_zeros = 1 leaves out entries that are exactly
+ * zero, as the S + transpose(S) step of SysmatAssemblerSparseSymm does
+ * (src/AssemblyModule.jl:576); 0 keeps the structural pattern (as
+ * SysmatAssemblerSparse's sparse() does). */
+int fegpu_matrix_nnz(fegpu_matrix *K, int drop_zeros, int64_t *nnz);
+int fegpu_matrix_copy_csc(fegpu_matrix *K, int drop_zeros, int64_t *colptr,
+                          int64_t *rowval, double *nzval);
+/* values only, in the structural pattern order (re-assembly on a fixed mesh) */
+int fegpu_matrix_copy_values(fegpu_matrix *K, double *nzval);
+/* y = K x on the device (host vectors of length nalldofs) */
+int fegpu_matrix_spmv(fegpu_matrix *K, const double *x, double *y);
+
+/* ---- generic assembler for element matrices formed on the host -----------
+ * startassembly! / assemble! / makematrix! of SysmatAssemblerSparse(Symm)
+ * (src/AssemblyModule.jl:209-329, 454-583) for FEMMs whose element matrices
+ * are computed by the caller: triples are buffered on the host, then sorted
+ * and reduced on the device into CSC (duplicates summed in input order). */
+int fegpu_assembler_create(fegpu_context *ctx, int symmetric, int64_t nrows,
+                           int64_t ncols, fegpu_assembler **out);
+int fegpu_assembler_destroy(fegpu_assembler *a);
+int fegpu_assembler_assemble(fegpu_assembler *a, const double *mat_colmajor,
+                             int nr, int nc, const int64_t *rows,
+                             const int64_t *cols);
+int fegpu_assembler_make(fegpu_assembler *a, int64_t *nnz);
+int fegpu_assembler_copy_csc(fegpu_assembler *a, int64_t *colptr,
+                             int64_t *rowval, double *nzval);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

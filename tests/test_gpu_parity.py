@@ -1,0 +1,393 @@
+"""GPU parity: libfegpu (through its C ABI) against the CPU oracle.
+
+Bar (FP64): the CSR structure is bit-exact; every value satisfies
+    |K_ij - Kref_ij| <= 1e-12 |Kref_ij| + 1e-14 max_k |Kref_ik|
+and |(K - Kref) x| <= 1e-12 |Kref x|.  The absolute term covers entries
+formed by cancellation (mathematically zero or nearly so, e.g. vertex /
+opposite mid-edge couplings of straight-edged T10 under an exact rule): any
+change of summation order, the reference's own LoopVectorization reordering
+included, moves them by a few ulps of the row scale.  Structure is compared
+on the structural pattern (SysmatAssemblerSparse semantics, zeros kept);
+the symmetric assembler's dropping of exact zeros depends on bitwise values
+and is checked on fully perturbed meshes, where no exact zeros arise.
+Mixed precision: normwise 1e-6.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+MIXED_TOL = 1e-6
+
+
+def _rowmax(K):
+    R = K.tocsr()
+    return np.maximum.reduceat(np.abs(R.data), R.indptr[:-1]) if R.nnz else np.zeros(0)
+
+
+RTOL = 1e-12
+ATOL_ROW = 1e-14
+
+
+def compare(K, Kr, tol=RTOL, structure=True, atol_row=ATOL_ROW):
+    """Returns (max raw relative error, max |dK| / (rtol |K| + atol row scale), |dK x|/|K x|)."""
+    K = K.tocsr()
+    K.sort_indices()
+    R = Kr.tocsr()
+    R.sort_indices()
+    same = np.array_equal(K.indptr, R.indptr) and np.array_equal(K.indices, R.indices)
+    if structure:
+        assert same, "CSR structure differs from the oracle's"
+    rm = np.repeat(_rowmax(R), np.diff(R.indptr))
+    if same:
+        diff = np.abs(K.data - R.data)
+    else:
+        A = (K - R).tocsr()
+        diff = np.abs(np.asarray(A[R.nonzero()]).ravel())
+        off = abs(A) - abs(A).multiply(R != 0)
+        if off.nnz:
+            rmax = _rowmax(R)
+            offr = off.tocsr()
+            for i in range(offr.shape[0]):
+                row = offr.data[offr.indptr[i]:offr.indptr[i + 1]]
+                if row.size:
+                    assert row.max() <= atol_row * rmax[i], "entry outside the oracle pattern"
+    raw = float((diff / np.maximum(np.abs(R.data), 1e-300)).max()) if diff.size else 0.0
+    gate = float((diff / (tol * np.abs(R.data) + atol_row * rm)).max()) if diff.size else 0.0
+    x = np.random.default_rng(7).uniform(-1, 1, K.shape[1])
+    kx = np.linalg.norm((K - R) @ x) / max(np.linalg.norm(R @ x), 1e-300)
+    assert gate <= 1.0, f"value error {gate:.3g} x the bound (raw relative {raw:.3e})"
+    assert kx <= tol, f"relative |dK x| {kx:.3e}"
+    return raw, gate, kx
+
+
+def _oracle_form(O, femm, form, geom, u, coef, kind=0, m=3, symmetric=True):
+    fes = femm.integdomain.fes
+    npts, Ns, dN, w, pc = femm.integdomain.integrationdata()
+    return O.bilform(form, fes.code, fes.conn, geom.values, u.dofnums, u.nalldofs(), pc, w, coef,
+                     coef_kind=kind, otherdim=femm.integdomain.otherdimension, m=m,
+                     symmetric=symmetric)
+
+
+def _field(ft, n, ndn):
+    return ft.numberdofs(ft.NodalField(np.zeros((n, ndn))))
+
+
+# ---------------------------------------------------------------- diffusion
+@pytest.mark.parametrize("et,n,rule", [("H8", 4, ("G", 3, 2)), ("H20", 3, ("G", 3, 3)),
+                                       ("T4", 3, ("T", 1)), ("T10", 3, ("T", 4)),
+                                       ("H8", 3, ("G", 3, 3)), ("T10", 2, ("T", 5))])
+@pytest.mark.parametrize("coef", ["iso", "general", "per_element"])
+def test_diffusion_fp64(ft, O, et, n, rule, coef):
+    gen = {"H8": ft.H8block, "H20": ft.H20block, "T4": ft.T4block, "T10": ft.T10block}[et]
+    fens, fes = gen(1.0, 1.2, 0.9, n, n + 1, n)
+    fens.xyz = ft.meshes.jitter_interior(fens.xyz, (n, n + 1, n), 0.2, 11, box=(1.0, 1.2, 0.9))
+    if et in ("H20", "T10"):
+        nv = fens.count()
+        fens = ft.meshes.recompute_midpoints(fens, fes, nv)
+    r = ft.GaussRule(*rule[1:]) if rule[0] == "G" else ft.TetRule(rule[1])
+    femm = ft.FEMMBase(ft.IntegDomain(fes, r))
+    geom = ft.NodalField(fens.xyz)
+    u = _field(ft, fens.count(), 1)
+    if coef == "iso":
+        cf, oc, kind = ft.DataCache(2.5), np.array([2.5]), 0
+    elif coef == "general":
+        k = np.array([[2.0, 0.3, 0.1], [0.3, 1.5, -0.2], [0.1, -0.2, 1.0]])
+        cf, oc, kind = ft.DataCache(k), k, 0
+    else:
+        v = np.random.default_rng(3).lognormal(0, 1, fes.count())
+        cf, oc, kind = ft.ElementwiseData(v), v.reshape(-1, 1), 1
+    K = ft.bilform_diffusion(femm, ft.SysmatAssemblerGPU(symmetric=False), geom, u, cf)
+    Kr = _oracle_form(O, femm, O.DIFFUSION, geom, u, oc, kind, symmetric=False)
+    compare(K, Kr)
+    assert abs(K - K.T).max() == 0.0
+    Ks = ft.bilform_diffusion(femm, geom, u, cf)
+    compare(Ks, _oracle_form(O, femm, O.DIFFUSION, geom, u, oc, kind), structure=False)
+
+
+# ---------------------------------------------------------------- elasticity
+@pytest.mark.parametrize("et,n,rule", [("H8", 3, ("G", 3, 2)), ("H20", 2, ("G", 3, 3)),
+                                       ("T4", 3, ("T", 1)), ("T10", 3, ("T", 4))])
+@pytest.mark.parametrize("coef", ["iso_const", "aniso_const", "per_element_iso", "per_element_D"])
+def test_elasticity_fp64(ft, O, et, n, rule, coef):
+    gen = {"H8": ft.H8block, "H20": ft.H20block, "T4": ft.T4block, "T10": ft.T10block}[et]
+    fens, fes = gen(1.0, 1.0, 1.0, n, n, n)
+    fens.xyz = ft.meshes.jitter_interior(fens.xyz, (n, n, n), 0.15, 5)
+    if et in ("H20", "T10"):
+        fens = ft.meshes.recompute_midpoints(fens, fes, 0)
+    r = ft.GaussRule(*rule[1:]) if rule[0] == "G" else ft.TetRule(rule[1])
+    femm = ft.FEMMBase(ft.IntegDomain(fes, r))
+    geom = ft.NodalField(fens.xyz)
+    u = _field(ft, fens.count(), 3)
+    rng = np.random.default_rng(9)
+    if coef == "iso_const":
+        D = ft.isotropic_D(210e9, 0.3)
+        cf, oc, kind = ft.DataCache(D), D, 0
+    elif coef == "aniso_const":
+        A = rng.uniform(-1, 1, (6, 6))
+        D = A @ A.T + 6 * np.eye(6)
+        cf, oc, kind = ft.DataCache(D), D, 0
+    elif coef == "per_element_iso":
+        E = rng.lognormal(np.log(70e9), 0.5, fes.count())
+        nu = rng.uniform(0.2, 0.35, fes.count())
+        cf = ft.IsotropicElementwise(E, nu)
+        oc = np.stack([ft.isotropic_D(a, b) for a, b in zip(E, nu)]).reshape(-1, 36)
+        kind = 1
+    else:
+        Ds = []
+        for _ in range(fes.count()):
+            A = rng.uniform(-1, 1, (6, 6))
+            Ds.append(A @ A.T + 6 * np.eye(6))
+        oc = np.stack(Ds).reshape(-1, 36)
+        cf, kind = ft.ElementwiseData(oc), 1
+    K = ft.bilform_lin_elastic(femm, ft.SysmatAssemblerGPU(symmetric=False), geom, u,
+                               ft.DeforModelRed3D, cf)
+    Kr = _oracle_form(O, femm, O.LIN_ELASTIC, geom, u, oc, kind, symmetric=False)
+    compare(K, Kr)
+    assert abs(K - K.T).max() == 0.0
+    Ks = ft.bilform_lin_elastic(femm, geom, u, ft.DeforModelRed3D, cf)
+    compare(Ks, _oracle_form(O, femm, O.LIN_ELASTIC, geom, u, oc, kind), structure=False)
+
+
+# ---------------------------------------------------------------- dot / linform
+@pytest.mark.parametrize("et,ndn", [("H8", 1), ("H8", 3), ("T10", 3), ("H20", 1)])
+def test_dot_volume(ft, O, et, ndn):
+    gen = {"H8": ft.H8block, "H20": ft.H20block, "T10": ft.T10block}[et]
+    fens, fes = gen(12.0, 1.1, 0.32, 2, 4, 3)
+    r = ft.TetRule(4) if et == "T10" else ft.GaussRule(3, 2)
+    femm = ft.FEMMBase(ft.IntegDomain(fes, r))
+    geom = ft.NodalField(fens.xyz)
+    u = _field(ft, fens.count(), ndn)
+    c = np.eye(ndn) * 1.7
+    if ndn == 3:
+        c[0, 1] = c[1, 0] = 0.2
+    for symmetric in (True, False):
+        asm = ft.SysmatAssemblerGPU(symmetric=symmetric)
+        K = ft.bilform_dot(femm, asm, geom, u, ft.DataCache(c))
+        Kr = _oracle_form(O, femm, O.DOT, geom, u, c, symmetric=symmetric)
+        compare(K, Kr, structure=not symmetric)
+    # test/test_forms.jl:1-27: v' G v = volume for the Gram matrix
+    G = ft.innerproduct(femm, geom, u)
+    v = np.ones(G.shape[0])
+    V = 12.0 * 1.1 * 0.32
+    assert abs(v @ G @ v - ndn * V) / V <= 1e-5
+
+
+def test_dot_surface_q4_thickness(ft, O):
+    """Q4 surface mass with thickness (IntegDomain(fes, rule, 0.01)), in 3-D
+    space (m = 3 -> surface Jacobian x thickness) and m = 2."""
+    fens, fes = ft.Q4block(2.0, 1.5, 5, 4)
+    rng = np.random.default_rng(1)
+    xyz = np.hstack([fens.xyz, rng.uniform(-0.05, 0.05, (fens.count(), 1))])
+    femm = ft.FEMMBase(ft.IntegDomain(fes, ft.GaussRule(2, 2), 0.01))
+    geom = ft.NodalField(xyz)
+    for ndn in (1, 3):
+        u = _field(ft, fens.count(), ndn)
+        for m in (2, 3):
+            K = ft.bilform_dot(femm, geom, u, ft.DataCache(np.eye(ndn)), m=m)
+            Kr = _oracle_form(O, femm, O.DOT, geom, u, np.eye(ndn), m=m)
+            compare(K, Kr, structure=False)
+
+
+def test_diffusion_q4_planar(ft, O):
+    """2-D diffusion with thickness (test/test_forms.jl:106-156 pattern on Q4)."""
+    fens, fes = ft.Q4block(12.0, 1.1, 6, 4)
+    femm = ft.FEMMBase(ft.IntegDomain(fes, ft.GaussRule(2, 2), 0.32))
+    geom = ft.NodalField(fens.xyz)
+    u = _field(ft, fens.count(), 1)
+    for cf, oc in ((ft.DataCache(1.0), np.array([1.0])), (ft.DataCache(np.eye(2)), np.eye(2))):
+        K = ft.bilform_diffusion(femm, geom, u, cf)
+        Kr = _oracle_form(O, femm, O.DIFFUSION, geom, u, oc)
+        compare(K, Kr, structure=False)
+    a, b, c = -0.1, 0.3, 0.4
+    v = a + b * fens.xyz[:, 0] + c * fens.xyz[:, 1]
+    V = 12.0 * 1.1 * 0.32
+    assert abs(v @ K @ v - (b * b + c * c) * V) / V <= 1e-5
+
+
+@pytest.mark.parametrize("et,ndn", [("H8", 1), ("T10", 3), ("H20", 3)])
+def test_linform(ft, O, et, ndn):
+    gen = {"H8": ft.H8block, "H20": ft.H20block, "T10": ft.T10block}[et]
+    fens, fes = gen(12.0, 1.1, 4.32, 2, 4, 3)
+    r = ft.TetRule(4) if et == "T10" else ft.GaussRule(3, 2)
+    femm = ft.FEMMBase(ft.IntegDomain(fes, r))
+    geom = ft.NodalField(fens.xyz)
+    P = _field(ft, fens.count(), ndn)
+    f = np.arange(1, ndn + 1) * 11.0
+    F = ft.linform_dot(femm, geom, P, ft.DataCache(f), 3)
+    npts, Ns, dN, w, pc = femm.integdomain.integrationdata()
+    Fr = O.linform_dot(fes.code, fes.conn, fens.xyz, P.dofnums, P.nalldofs(), pc, w, f)
+    assert np.abs(F - Fr).max() <= 1e-12 * np.abs(Fr).max()
+    # test/test_forms.jl:158-194: sum(F) = volume * force
+    F = ft.distribloads(femm, geom, P, ft.ForceIntensity(f), 3)
+    V = 12.0 * 1.1 * 4.32
+    assert abs(F.sum() - V * f.sum()) / (V * f.sum()) <= 1e-5
+
+
+# ---------------------------------------------------------------- numbering, determinism
+def test_general_dof_numbering_with_ebcs(ft, O):
+    """Fixed DOFs numbered last (non-contiguous per node): general slot path."""
+    fens, fes = ft.T10block(1.0, 1.0, 1.0, 2, 3, 2)
+    femm = ft.FEMMBase(ft.IntegDomain(fes, ft.TetRule(4)))
+    geom = ft.NodalField(fens.xyz)
+    u = ft.NodalField(np.zeros((fens.count(), 3)))
+    on_face = np.flatnonzero(np.abs(fens.xyz[:, 0]) < 1e-12) + 1
+    ft.setebc(u, on_face, True, [1], 0.0)
+    ft.setebc(u, on_face[::2], True, [3], 0.0)
+    ft.numberdofs(u)
+    D = ft.isotropic_D(1.0, 0.25)
+    K = ft.bilform_lin_elastic(femm, ft.SysmatAssemblerGPU(symmetric=False), geom, u,
+                               ft.DeforModelRed3D, ft.DataCache(D))
+    Kr = _oracle_form(O, femm, O.LIN_ELASTIC, geom, u, D, symmetric=False)
+    compare(K, Kr)
+
+
+def test_permuted_node_numbering(ft, O):
+    fens, fes = ft.H8block(1.0, 1.0, 1.0, 3, 3, 3)
+    u = ft.NodalField(np.zeros((fens.count(), 3)))
+    perm = np.random.default_rng(4).permutation(fens.count()) + 1
+    ft.numberdofs(u, entperm=perm)
+    femm = ft.FEMMBase(ft.IntegDomain(fes, ft.GaussRule(3, 2)))
+    geom = ft.NodalField(fens.xyz)
+    D = ft.isotropic_D(3.0, 0.2)
+    K = ft.bilform_lin_elastic(femm, geom, u, ft.DeforModelRed3D, ft.DataCache(D))
+    Kr = _oracle_form(O, femm, O.LIN_ELASTIC, geom, u, D)
+    compare(K, Kr, structure=False)
+
+
+def test_determinism(ft):
+    """test/test_basics.jl:3043-3045: repeated assembly is bitwise identical."""
+    fens, fes = ft.t10_elastic_mesh(n=4)
+    femm = ft.FEMMBase(ft.IntegDomain(fes, ft.TetRule(4)))
+    geom = ft.NodalField(fens.xyz)
+    u = _field(ft, fens.count(), 3)
+    D = ft.isotropic_D(210e9, 0.3)
+    asm = ft.SysmatAssemblerGPU(result="device")
+    v1 = ft.bilform_lin_elastic(femm, asm, geom, u, ft.DeforModelRed3D, ft.DataCache(D)).values()
+    v2 = ft.bilform_lin_elastic(femm, asm, geom, u, ft.DeforModelRed3D, ft.DataCache(D)).values()
+    assert np.array_equal(v1, v2)
+
+
+def test_colouring_matches_reference(ft, O, kats):
+    k = kats["coloring_t4"]
+    fens, fes = ft.T4block(*k["block"])
+    femm = ft.FEMMBase(ft.IntegDomain(fes, ft.TetRule(1)))
+    femm.set_geometry(ft.NodalField(fens.xyz))
+    col, nc = femm.colors()
+    ref, nref = O.element_coloring(fes.conn, fens.count())
+    assert nc == nref == len(k["unique_colors_in_order"])
+    assert np.array_equal(col, ref)
+
+
+def test_connection_matrix_degree(ft, kats):
+    k = kats["connection_degree"]
+    fens, fes = ft.H8block(*k["block"])
+    femm = ft.FEMMBase(ft.IntegDomain(fes, ft.GaussRule(3, 2)))
+    C = ft.connectionmatrix(femm, fens.count())
+    deg = np.diff(C.indptr)
+    assert deg.max() == k["max_degree"] and deg.min() == k["min_degree"]
+
+
+def test_zero_dropping_on_regular_mesh(ft, O):
+    """On a regular block exact zeros appear; symmetric semantics drop the ones
+    the oracle's S + S' drops when the values agree bitwise, and the
+    structural (keep-zeros) result matches the oracle's sparse() pattern."""
+    fens, fes = ft.H8block(1.0, 1.0, 1.0, 3, 3, 3)
+    femm = ft.FEMMBase(ft.IntegDomain(fes, ft.GaussRule(3, 2)))
+    geom = ft.NodalField(fens.xyz)
+    u = _field(ft, fens.count(), 1)
+    K = ft.bilform_diffusion(femm, ft.SysmatAssemblerGPU(symmetric=False), geom, u,
+                             ft.DataCache(1.0))
+    Kr = _oracle_form(O, femm, O.DIFFUSION, geom, u, np.array([1.0]), symmetric=False)
+    compare(K, Kr)
+
+
+@pytest.mark.parametrize("et", ["H8", "T10", "H20"])
+def test_symmetric_structure_fully_perturbed(ft, O, et):
+    """Every node moved: no exact zeros, so the S + S' zero dropping of the
+    symmetric assembler leaves the structural pattern, bit-exactly."""
+    gen = {"H8": ft.H8block, "H20": ft.H20block, "T10": ft.T10block}[et]
+    fens, fes = gen(1.0, 1.0, 1.0, 3, 2, 3)
+    rng = np.random.default_rng(12)
+    fens.xyz = fens.xyz + rng.uniform(-0.05, 0.05, fens.xyz.shape)
+    if et != "H8":
+        fens = ft.meshes.recompute_midpoints(fens, fes, 0)
+    r = ft.TetRule(4) if et == "T10" else ft.GaussRule(3, 3 if et == "H20" else 2)
+    femm = ft.FEMMBase(ft.IntegDomain(fes, r))
+    geom = ft.NodalField(fens.xyz)
+    u = _field(ft, fens.count(), 3)
+    D = ft.isotropic_D(210e9, 0.3)
+    K = ft.bilform_lin_elastic(femm, geom, u, ft.DeforModelRed3D, ft.DataCache(D))
+    npts, Ns, dN, w, pc = femm.integdomain.integrationdata()
+    Kr, dropped, _ = O.bilform(O.LIN_ELASTIC, fes.code, fes.conn, geom.values, u.dofnums,
+                               u.nalldofs(), pc, w, D, phases=True)
+    assert dropped == 0
+    compare(K, Kr)
+
+
+# ---------------------------------------------------------------- generic assembler
+def test_generic_assembler_kats(ft, kats):
+    k = kats["assembler"]["sparse_rect"]
+    a = ft.SysmatAssemblerGPU(symmetric=False)
+    a.startassembly(5, 5, 3, 7, 7)
+    for m, r, c in zip(k["mats"], k["rows"], k["cols"]):
+        a.assemble(np.array(m), r, c)
+    A = a.makematrix().toarray()
+    assert np.abs(np.array(k["expected"]) - A).max() < 1e-5
+    k = kats["assembler"]["symm_mtm"]
+    a = ft.SysmatAssemblerGPU(symmetric=True)
+    a.startassembly(5, 5, 3, 7, 7)
+    for m, r, c in zip(k["mats"], k["rows"], k["cols"]):
+        m = np.array(m)
+        a.assemble(m.T @ m, r, c)
+    A = a.makematrix().toarray()
+    assert np.abs(np.array(k["expected"]) - A).max() < 1e-5
+    assert np.abs(A - A.T).max() == 0.0
+
+
+def test_generic_assembler_random(ft, O):
+    """test/test_basics.jl:2100-2175: random symmetric matrices vs the oracle."""
+    rng = np.random.default_rng(2)
+    N = 133
+    for symm in (False, True):
+        a = ft.SysmatAssemblerGPU(symmetric=symm)
+        a.startassembly(6, 6, 100, N, N)
+        o = O.Assembler(symm, N, N)
+        for _ in range(200):
+            k = int(rng.integers(2, 7))
+            M = rng.uniform(-1, 1, (k, k))
+            M = M + M.T
+            d = rng.permutation(N)[:k] + 1
+            a.assemble(M, d, d)
+            o.assemble(M, d, d)
+        A = a.makematrix()
+        Ar = o.make()
+        compare(A, Ar)
+
+
+# ---------------------------------------------------------------- mixed precision
+@pytest.mark.parametrize("et", ["H20", "T10", "H8"])
+def test_mixed_precision(ft, O, et):
+    if et == "H20":
+        fens, fes, flagged = ft.h20_elastic_mesh(n=4, distort_fraction=0.05)
+        r = ft.GaussRule(3, 3)
+    elif et == "T10":
+        fens, fes = ft.t10_elastic_mesh(n=4)
+        r = ft.TetRule(4)
+    else:
+        fens, fes = ft.h8_diffusion_mesh(n=5)
+        r = ft.GaussRule(3, 2)
+    femm = ft.FEMMBase(ft.IntegDomain(fes, r))
+    geom = ft.NodalField(fens.xyz)
+    u = _field(ft, fens.count(), 3)
+    rng = np.random.default_rng(4)
+    E = rng.lognormal(np.log(70e9), 0.5, fes.count())
+    nu = rng.uniform(0.2, 0.35, fes.count())
+    cf = ft.IsotropicElementwise(E, nu)
+    K64 = ft.bilform_lin_elastic(femm, ft.SysmatAssemblerGPU(), geom, u, ft.DeforModelRed3D, cf)
+    K32 = ft.bilform_lin_elastic(femm, ft.SysmatAssemblerGPU(precision="mixed"), geom, u,
+                                 ft.DeforModelRed3D, cf)
+    x = rng.uniform(-1, 1, K64.shape[0])
+    assert np.linalg.norm((K32 - K64) @ x) / np.linalg.norm(K64 @ x) <= MIXED_TOL
+    assert abs(K32 - K64).max() / abs(K64).max() <= MIXED_TOL
+    assert abs(K32 - K32.T).max() == 0.0
