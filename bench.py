@@ -305,6 +305,12 @@ def run_ours(args):
     ft = entry.load_package()
     lib = Lib(ft, local)
     stream = torch.cuda.ExternalStream(lib.stream, device=local)
+    if args.only in ("h20", "h8"):
+        fn = bench_h20 if args.only == "h20" else bench_h8
+        res = fn(ft, torch, lib, stream, args, local, dist)
+        if rank == 0:
+            print(json.dumps({"only": args.only, "workload": res}), flush=True)
+        return
 
     # ---------------- headline: T10 60^3, FP64
     t0 = time.perf_counter()
@@ -377,7 +383,7 @@ def run_ours(args):
     torch.cuda.empty_cache()
 
     workloads = {}
-    if not args.headline_only:
+    if not args.headline_only and args.only is None:
         workloads["h20_40_elasticity"] = bench_h20(ft, torch, lib, stream, args, local, dist)
         workloads["h8_20_diffusion"] = bench_h8(ft, torch, lib, stream, args, local, dist)
 
@@ -425,7 +431,7 @@ def run_ours(args):
 
 
 def bench_h20(ft, torch, lib, stream, args, local, dist):
-    fens, fes, flagged = ft.h20_elastic_mesh(n=H20_N)
+    fens, fes, flagged = ft.h20_elastic_mesh(n=args.h20_n)
     rng = np.random.default_rng(4)
     E = rng.lognormal(np.log(70e9), 0.5, fes.count())
     nu = rng.uniform(0.2, 0.35, fes.count())
@@ -503,6 +509,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--headline-only", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--only", choices=["t10", "h20", "h8"], default=None,
+                    help="run one workload only (profiling); prints its numbers")
+    ap.add_argument("--h20-n", type=int, default=H20_N)
     ap.add_argument("--t10-n", type=int, default=T10_N,
                     help="cells per side of the headline T10 block (60 = the benchmark size)")
     args = ap.parse_args()

@@ -129,7 +129,7 @@ void validate_conn(const int64_t *conn, int64_t nelem, int nne, int64_t nnodes,
 // Copies the caller's coefficient into KArgs (constant) or a device array in
 // colour order (per element / per point).
 void stage_coef(fegpu_femm *fm, const fegpu_coef *cf, int expect_ncomp, KArgs &a,
-                CoefStage &st) {
+                CoefStage &st, bool colour_order = true) {
   FEGPU_REQUIRE(cf != nullptr && cf->data != nullptr, "coefficient: null data");
   a.coef_kind = cf->kind;
   a.ncomp = cf->ncomp;
@@ -150,6 +150,10 @@ void stage_coef(fegpu_femm *fm, const fegpu_coef *cf, int expect_ncomp, KArgs &a
   st.raw.alloc(sizeof(double) * n);
   st.sorted.alloc(sizeof(double) * n);
   FEGPU_CUDA(cudaMemcpyAsync(st.raw.p, cf->data, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  if (!colour_order) {
+    a.coef = st.raw.as<double>();
+    return;
+  }
   k_gather_rows<<<grid_of(n), 256, 0, s>>>(st.raw.as<double>(), fm->perm.as<int32_t>(),
                                            fm->nelem, width, st.sorted.as<double>());
   FEGPU_CUDA(cudaGetLastError());
@@ -198,6 +202,59 @@ void run_colours(fegpu_dofmap *dm, int form, int precision, KArgs &a) {
     FEGPU_CUDA(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
     ctx->kernel_ms += ms;
   }
+}
+
+// Mixed precision: element blocks in FP32 into the ring, then the row gather
+// (gather.cu), chunk by chunk in element order.
+void run_gather(fegpu_dofmap *dm, int form, KArgs &a) {
+  fegpu_femm *fm = dm->femm;
+  fegpu_context *ctx = fm->ctx;
+  const int nne = fm->nne, ndn = dm->ndn;
+  const int bs = ndn * ndn, nblk = nne * (nne + 1) / 2;
+  if (!dm->gather_ready) build_gather_plan(dm, nblk * bs);
+  a.conn = fm->conn_orig.as<int32_t>();
+  a.te = choose_tile(fm->etype, form, FEGPU_MIXED, fm->npts);
+  const size_t smem = form_smem_bytes(fm->etype, form, FEGPU_MIXED, fm->npts, a.te);
+  FEGPU_REQUIRE(smem <= 227 * 1024, "quadrature rule too large for the element kernel");
+  GArgs g;
+  g.n2e_ptr = dm->n2e_ptr.as<int64_t>();
+  g.n2e_elem = dm->n2e_elem.as<int32_t>();
+  g.n2e_loc = dm->n2e_loc.as<uint8_t>();
+  g.nodes = dm->gnodes.as<int32_t>();
+  g.nptr = dm->nptr.as<int64_t>();
+  g.pos = dm->pos_orig.as<uint16_t>();
+  g.ke = dm->ke.as<float>();
+  g.chunk = dm->chunk;
+  g.ring = dm->ring;
+  g.dof = dm->dof.as<int32_t>();
+  g.rowptr = dm->rowptr.as<int64_t>();
+  g.colperm = dm->contiguous ? nullptr : dm->colperm.as<int32_t>();
+  g.cpoff = dm->contiguous ? nullptr : dm->cpoff.as<int64_t>();
+  g.val = a.val;
+  g.maxdeg = dm->maxdeg;
+  const int64_t nch = static_cast<int64_t>(dm->chunk_nodes.size()) - 1;
+  if (ctx->timing) FEGPU_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
+  for (int64_t c = 0; c < nch; ++c) {
+    a.e0 = c * dm->chunk;
+    a.e1 = std::min(fm->nelem, (c + 1) * dm->chunk);
+    a.ke = dm->ke.as<float>() + (c % dm->ring) * dm->chunk * nblk * bs;
+    ctx->launches += launch_form(fm->etype, form, FEGPU_MIXED, ndn, a, ctx->num_sms, ctx->stream);
+    g.n0 = dm->chunk_nodes[c];
+    g.n1 = dm->chunk_nodes[c + 1];
+    ctx->launches += launch_gather(fm->etype, ndn, g, ctx->num_sms, ctx->stream);
+  }
+  if (ctx->timing) {
+    FEGPU_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
+    FEGPU_CUDA(cudaEventSynchronize(ctx->ev1));
+    float ms = 0.f;
+    FEGPU_CUDA(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+    ctx->kernel_ms += ms;
+  }
+}
+
+void run_form(fegpu_dofmap *dm, int form, int precision, KArgs &a) {
+  if (precision == FEGPU_MIXED && form <= F_ELAST_GEN) run_gather(dm, form, a);
+  else run_colours(dm, form, precision, a);
 }
 
 void require_geometry(fegpu_femm *fm) {
@@ -341,6 +398,7 @@ int fegpu_femm_create(fegpu_context *ctx, int etype, int64_t nelem, const int64_
       std::memcpy(&cs[p * nne], &c0[e * nne], sizeof(int32_t) * nne);
     }
     fm->color_offsets = off;
+    fm->conn_host = c0;
     cudaStream_t s = ctx->stream;
     fm->conn_orig.alloc(sizeof(int32_t) * c0.size());
     fm->conn.alloc(sizeof(int32_t) * cs.size());
@@ -518,9 +576,10 @@ int fegpu_bilform_diffusion(fegpu_matrix *K, const fegpu_coef *cf, int precision
     }
     KArgs a = base_args(K, dm);
     CoefStage st;
-    stage_coef(fm, cf, cf->ncomp, a, st);
-    zero_matrix(K);
-    if (fm->nelem > 0) run_colours(dm, form, precision, a);
+    const bool gather = precision == FEGPU_MIXED;
+    stage_coef(fm, cf, cf->ncomp, a, st, !gather);
+    if (!gather) zero_matrix(K);
+    if (fm->nelem > 0) run_form(dm, form, precision, a);
     FEGPU_CUDA(cudaStreamSynchronize(fm->ctx->stream));  // st owns the staged data
   });
 }
@@ -538,9 +597,10 @@ int fegpu_bilform_lin_elastic(fegpu_matrix *K, const fegpu_coef *cf, int precisi
     KArgs a = base_args(K, dm);
     CoefStage st;
     int form;
+    const bool gather = precision == FEGPU_MIXED;
     if (cf->kind == FEGPU_COEF_ISO_LAME) {
       form = F_ELAST_ISO;
-      stage_coef(fm, cf, 2, a, st);
+      stage_coef(fm, cf, 2, a, st, !gather);
     } else if (cf->kind == FEGPU_COEF_CONST && cf->ncomp == 36) {
       double lam, mu;
       if (is_isotropic(cf->data, lam, mu)) {
@@ -551,18 +611,18 @@ int fegpu_bilform_lin_elastic(fegpu_matrix *K, const fegpu_coef *cf, int precisi
         a.cconst[1] = mu;
       } else {
         form = F_ELAST_GEN;
-        stage_coef(fm, cf, 36, a, st);
+        stage_coef(fm, cf, 36, a, st, !gather);
       }
     } else if (cf->kind == FEGPU_COEF_PER_ELEMENT && cf->ncomp == 36) {
       form = F_ELAST_GEN;
-      stage_coef(fm, cf, 36, a, st);
+      stage_coef(fm, cf, 36, a, st, !gather);
     } else {
       throw Error{FEGPU_ERR_ARG,
                   "lin_elastic: coefficient must be a 6x6 D (constant or per element) or "
                   "per-element (lambda, mu)"};
     }
-    zero_matrix(K);
-    if (fm->nelem > 0) run_colours(dm, form, precision, a);
+    if (!gather) zero_matrix(K);
+    if (fm->nelem > 0) run_form(dm, form, precision, a);
     FEGPU_CUDA(cudaStreamSynchronize(fm->ctx->stream));
   });
 }

@@ -92,25 +92,28 @@ __host__ __device__ constexpr int voigt_sel(int i, int m) {
 // (no contraction into FMA), so the element arithmetic follows the
 // reference's expressions operation by operation; in FP32 contraction is
 // allowed (it only adds accuracy).
-template <typename C>
+// EX selects the exact (uncontracted) FP64 form; the elasticity kernels,
+// whose contraction order is their own anyway, use fused FP64 multiply-adds
+// (half the FP64 instructions on a part whose FP64 rate is 1/64 of FP32).
+template <typename C, bool EX = true>
 __device__ __forceinline__ C mul(C a, C b) {
-  if constexpr (std::is_same<C, double>::value) return __dmul_rn(a, b);
+  if constexpr (std::is_same<C, double>::value && EX) return __dmul_rn(a, b);
   else return a * b;
 }
-template <typename C>
+template <typename C, bool EX = true>
 __device__ __forceinline__ C add(C a, C b) {
-  if constexpr (std::is_same<C, double>::value) return __dadd_rn(a, b);
+  if constexpr (std::is_same<C, double>::value && EX) return __dadd_rn(a, b);
   else return a + b;
 }
-template <typename C>
+template <typename C, bool EX = true>
 __device__ __forceinline__ C sub(C a, C b) {
-  if constexpr (std::is_same<C, double>::value) return __dsub_rn(a, b);
+  if constexpr (std::is_same<C, double>::value && EX) return __dsub_rn(a, b);
   else return a - b;
 }
-template <typename C>
+template <typename C, bool EX = true>
 __device__ __forceinline__ C madd(C a, C b, C c) {  // c + a*b
-  if constexpr (std::is_same<C, double>::value) return __dadd_rn(c, __dmul_rn(a, b));
-  else return fmaf(a, b, c);
+  if constexpr (std::is_same<C, double>::value && EX) return __dadd_rn(c, __dmul_rn(a, b));
+  else return fma(a, b, c);
 }
 
 // Geometry at one quadrature point, computed in C (double or float):
@@ -118,7 +121,7 @@ __device__ __forceinline__ C madd(C a, C b, C c) {  // c + a*b
 // (src/FESetModule.jl:426-435, 479-489) and gradN! (453-470, 507-544).
 // Writes the spatial gradients (as T) and returns the measure Jacobian
 // (times the other dimension when a two-manifold is integrated as a volume).
-template <int NNE, int MDIM, bool GRAD, typename C, typename T>
+template <int NNE, int MDIM, bool GRAD, typename C, typename T, bool EX = true>
 __device__ __forceinline__ C geometry_qp(const double *X, const double *dN, int sdim,
                                          int measure_volume, double otherdim, T *g,
                                          float *det_out) {
@@ -139,46 +142,46 @@ __device__ __forceinline__ C geometry_qp(const double *X, const double *dN, int 
     for (int m = 0; m < MDIM; ++m) {
       const C d = C(dN[k * MDIM + m]);
 #pragma unroll
-      for (int s = 0; s < 3; ++s) J[s][m] = madd(x[s], d, J[s][m]);
+      for (int s = 0; s < 3; ++s) J[s][m] = madd<C, EX>(x[s], d, J[s][m]);
     }
   }
   C inv[MDIM][MDIM];
   C Jac;
   if constexpr (MDIM == 3) {
-    const C c0 = sub(mul(J[1][1], J[2][2]), mul(J[2][1], J[1][2]));
-    const C c1 = sub(mul(J[1][0], J[2][2]), mul(J[1][2], J[2][0]));
-    const C c2 = sub(mul(J[1][0], J[2][1]), mul(J[1][1], J[2][0]));
-    const C det = add(sub(mul(J[0][0], c0), mul(J[0][1], c1)), mul(J[0][2], c2));
+    const C c0 = sub<C, EX>(mul<C, EX>(J[1][1], J[2][2]), mul<C, EX>(J[2][1], J[1][2]));
+    const C c1 = sub<C, EX>(mul<C, EX>(J[1][0], J[2][2]), mul<C, EX>(J[1][2], J[2][0]));
+    const C c2 = sub<C, EX>(mul<C, EX>(J[1][0], J[2][1]), mul<C, EX>(J[1][1], J[2][0]));
+    const C det = add<C, EX>(sub<C, EX>(mul<C, EX>(J[0][0], c0), mul<C, EX>(J[0][1], c1)), mul<C, EX>(J[0][2], c2));
     Jac = det;
     if (GRAD) {
       const C id = C(1) / det;
-      inv[0][0] = mul(c0, id);
-      inv[0][1] = mul(-sub(mul(J[0][1], J[2][2]), mul(J[0][2], J[2][1])), id);
-      inv[0][2] = mul(sub(mul(J[0][1], J[1][2]), mul(J[0][2], J[1][1])), id);
-      inv[1][0] = mul(-c1, id);
-      inv[1][1] = mul(sub(mul(J[0][0], J[2][2]), mul(J[0][2], J[2][0])), id);
-      inv[1][2] = mul(-sub(mul(J[0][0], J[1][2]), mul(J[1][0], J[0][2])), id);
-      inv[2][0] = mul(sub(mul(J[1][0], J[2][1]), mul(J[2][0], J[1][1])), id);
-      inv[2][1] = mul(-sub(mul(J[0][0], J[2][1]), mul(J[2][0], J[0][1])), id);
-      inv[2][2] = mul(sub(mul(J[0][0], J[1][1]), mul(J[1][0], J[0][1])), id);
+      inv[0][0] = mul<C, EX>(c0, id);
+      inv[0][1] = mul<C, EX>(-sub<C, EX>(mul<C, EX>(J[0][1], J[2][2]), mul<C, EX>(J[0][2], J[2][1])), id);
+      inv[0][2] = mul<C, EX>(sub<C, EX>(mul<C, EX>(J[0][1], J[1][2]), mul<C, EX>(J[0][2], J[1][1])), id);
+      inv[1][0] = mul<C, EX>(-c1, id);
+      inv[1][1] = mul<C, EX>(sub<C, EX>(mul<C, EX>(J[0][0], J[2][2]), mul<C, EX>(J[0][2], J[2][0])), id);
+      inv[1][2] = mul<C, EX>(-sub<C, EX>(mul<C, EX>(J[0][0], J[1][2]), mul<C, EX>(J[1][0], J[0][2])), id);
+      inv[2][0] = mul<C, EX>(sub<C, EX>(mul<C, EX>(J[1][0], J[2][1]), mul<C, EX>(J[2][0], J[1][1])), id);
+      inv[2][1] = mul<C, EX>(-sub<C, EX>(mul<C, EX>(J[0][0], J[2][1]), mul<C, EX>(J[2][0], J[0][1])), id);
+      inv[2][2] = mul<C, EX>(sub<C, EX>(mul<C, EX>(J[0][0], J[1][1]), mul<C, EX>(J[1][0], J[0][1])), id);
     }
   } else {
     if (sdim == 2) {
-      Jac = sub(mul(J[0][0], J[1][1]), mul(J[1][0], J[0][1]));
+      Jac = sub<C, EX>(mul<C, EX>(J[0][0], J[1][1]), mul<C, EX>(J[1][0], J[0][1]));
     } else {  // |J1 x J2|
-      const C c1 = sub(mul(J[1][0], J[2][1]), mul(J[2][0], J[1][1]));
-      const C c2 = sub(mul(J[2][0], J[0][1]), mul(J[0][0], J[2][1]));
-      const C c3 = sub(mul(J[0][0], J[1][1]), mul(J[1][0], J[0][1]));
-      Jac = sqrt(add(add(mul(c1, c1), mul(c2, c2)), mul(c3, c3)));
+      const C c1 = sub<C, EX>(mul<C, EX>(J[1][0], J[2][1]), mul<C, EX>(J[2][0], J[1][1]));
+      const C c2 = sub<C, EX>(mul<C, EX>(J[2][0], J[0][1]), mul<C, EX>(J[0][0], J[2][1]));
+      const C c3 = sub<C, EX>(mul<C, EX>(J[0][0], J[1][1]), mul<C, EX>(J[1][0], J[0][1]));
+      Jac = sqrt(add<C, EX>(add<C, EX>(mul<C, EX>(c1, c1), mul<C, EX>(c2, c2)), mul<C, EX>(c3, c3)));
     }
     if (GRAD) {
-      const C id = C(1) / sub(mul(J[0][0], J[1][1]), mul(J[0][1], J[1][0]));
-      inv[0][0] = mul(J[1][1], id);
-      inv[0][1] = mul(-J[0][1], id);
-      inv[1][0] = mul(-J[1][0], id);
-      inv[1][1] = mul(J[0][0], id);
+      const C id = C(1) / sub<C, EX>(mul<C, EX>(J[0][0], J[1][1]), mul<C, EX>(J[0][1], J[1][0]));
+      inv[0][0] = mul<C, EX>(J[1][1], id);
+      inv[0][1] = mul<C, EX>(-J[0][1], id);
+      inv[1][0] = mul<C, EX>(-J[1][0], id);
+      inv[1][1] = mul<C, EX>(J[0][0], id);
     }
-    if (measure_volume) Jac = mul(Jac, C(otherdim));
+    if (measure_volume) Jac = mul<C, EX>(Jac, C(otherdim));
   }
   if (det_out) *det_out = float(Jac);
   if (GRAD) {
@@ -186,9 +189,9 @@ __device__ __forceinline__ C geometry_qp(const double *X, const double *dN, int 
     for (int k = 0; k < NNE; ++k)
 #pragma unroll
       for (int c = 0; c < MDIM; ++c) {
-        C v = mul(C(dN[k * MDIM]), inv[0][c]);
+        C v = mul<C, EX>(C(dN[k * MDIM]), inv[0][c]);
 #pragma unroll
-        for (int m = 1; m < MDIM; ++m) v = madd(C(dN[k * MDIM + m]), inv[m][c], v);
+        for (int m = 1; m < MDIM; ++m) v = madd<C, EX>(C(dN[k * MDIM + m]), inv[m][c], v);
         g[k * MDIM + c] = T(v);
       }
   }
@@ -228,9 +231,9 @@ __device__ __forceinline__ void qp_weights(const KArgs &a, int64_t es, int q, in
       }
     *jw = Jw;
   } else if constexpr (FORM == F_ELAST_ISO || FORM == F_ELAST_GEN) {
-    const T Jw = mul(Jac, T(wq));
+    const T Jw = Jac * T(wq);
 #pragma unroll
-    for (int k = 0; k < NNE * MDIM; ++k) wg[k] = mul(Jw, g[k]);
+    for (int k = 0; k < NNE * MDIM; ++k) wg[k] = Jw * g[k];
     *jw = Jw;
   } else if constexpr (FORM == F_DOT) {
     *jw = Jac;
@@ -245,6 +248,7 @@ __global__ void __launch_bounds__(kFormThreads) k_form(const KArgs a) {
   constexpr bool GRAD = FORM <= F_ELAST_GEN;
   constexpr int NBLK = NNE * (NNE + 1) / 2;
   constexpr bool MIXED = std::is_same<T, float>::value;
+  constexpr bool EXACT = !(FORM == F_ELAST_ISO || FORM == F_ELAST_GEN);
   extern __shared__ __align__(16) unsigned char smem[];
   const int npts = a.npts, te = a.te;
   const SmemLayout L = smem_layout(NNE, MDIM, npts, te, sizeof(T), GRAD);
@@ -293,7 +297,7 @@ __global__ void __launch_bounds__(kFormThreads) k_form(const KArgs a) {
       const int e = i / npts, q = i - e * npts;
       T *g = sG + (static_cast<size_t>(e) * npts + q) * NNE * MDIM;
       T *wg = sWG + (static_cast<size_t>(e) * npts + q) * NNE * MDIM;
-      const T Jac = T(geometry_qp<NNE, MDIM, GRAD, T, T>(sX + e * NNE * 3, sdN + q * NNE * MDIM,
+      const T Jac = T(geometry_qp<NNE, MDIM, GRAD, T, T, EXACT>(sX + e * NNE * 3, sdN + q * NNE * MDIM,
                                                          a.sdim, vol, a.otherdim, g,
                                                          sDet + e * npts + q));
       qp_weights<NNE, MDIM, FORM, T>(a, eb + e, q, npts, Jac, sw[q], g, wg, sJw + e * npts + q);
@@ -313,7 +317,7 @@ __global__ void __launch_bounds__(kFormThreads) k_form(const KArgs a) {
         if (!(dmin > static_cast<float>(a.distort_tol) * dmax)) {
           T *g = sG + (static_cast<size_t>(e) * npts + q) * NNE * MDIM;
           T *wg = sWG + (static_cast<size_t>(e) * npts + q) * NNE * MDIM;
-          const T Jac = T(geometry_qp<NNE, MDIM, GRAD, double, T>(
+          const T Jac = T(geometry_qp<NNE, MDIM, GRAD, double, T, EXACT>(
               sX + e * NNE * 3, sdN + q * NNE * MDIM, a.sdim, vol, a.otherdim, g, nullptr));
           qp_weights<NNE, MDIM, FORM, T>(a, eb + e, q, npts, Jac, sw[q], g, wg,
                                          sJw + e * npts + q);
@@ -352,8 +356,9 @@ __global__ void __launch_bounds__(kFormThreads) k_form(const KArgs a) {
       const int e = i / NBLK, blk = i - e * NBLK;
       const int pa = sPair[2 * blk], pb = sPair[2 * blk + 1];
       const int64_t es = eb + e;
-      double V[NDN][NDN];   // K[(A,i),(B,j)]
-      double Vt[NDN][NDN];  // K[(B,j),(A,i)] stored as [j][i]
+      using VT = typename std::conditional<GRAD, T, double>::type;
+      VT V[NDN][NDN];   // K[(A,i),(B,j)]
+      VT Vt[NDN][NDN];  // K[(B,j),(A,i)] stored as [j][i]
       if constexpr (FORM == F_DIFF_ISO || FORM == F_DIFF_GEN) {
         // Ke[a, b] += g_a . WG_b, point by point (row a <= column b)
         const T *ga = sG + (static_cast<size_t>(e) * npts) * NNE * MDIM + pa * MDIM;
@@ -372,8 +377,8 @@ __global__ void __launch_bounds__(kFormThreads) k_form(const KArgs a) {
             s = add(s, acc);
           }
         }
-        V[0][0] = double(s);
-        Vt[0][0] = V[0][0];
+        V[0][0] = s;
+        Vt[0][0] = s;
       } else if constexpr (FORM == F_ELAST_ISO || FORM == F_ELAST_GEN) {
         // Gram matrix of the gradients: M^{mn} = sum_q (Jac w) g_am g_bn
         T M[3][3];
@@ -393,24 +398,24 @@ __global__ void __launch_bounds__(kFormThreads) k_form(const KArgs a) {
 #pragma unroll
           for (int m = 0; m < 3; ++m)
 #pragma unroll
-            for (int n = 0; n < 3; ++n) M[m][n] = madd(x[m], y[n], M[m][n]);
+            for (int n = 0; n < 3; ++n) M[m][n] = fma(x[m], y[n], M[m][n]);
         }
         if constexpr (FORM == F_ELAST_ISO) {
-          double lam, mu;
+          T lam, mu;
           if (a.coef_kind == FEGPU_COEF_ISO_LAME) {
-            lam = a.coef[2 * es];
-            mu = a.coef[2 * es + 1];
+            lam = T(a.coef[2 * es]);
+            mu = T(a.coef[2 * es + 1]);
           } else {
-            lam = a.cconst[0];
-            mu = a.cconst[1];
+            lam = T(a.cconst[0]);
+            mu = T(a.cconst[1]);
           }
-          const double tr = double(M[0][0]) + double(M[1][1]) + double(M[2][2]);
+          const T mtr = mu * (M[0][0] + M[1][1] + M[2][2]);
 #pragma unroll
           for (int ii = 0; ii < 3; ++ii)
 #pragma unroll
             for (int jj = 0; jj < 3; ++jj) {
-              double v = lam * double(M[ii][jj]) + mu * double(M[jj][ii]);
-              if (ii == jj) v += mu * tr;
+              T v = fma(lam, M[ii][jj], mu * M[jj][ii]);
+              if (ii == jj) v += mtr;
               V[ii][jj] = v;
             }
         } else {
@@ -419,12 +424,12 @@ __global__ void __launch_bounds__(kFormThreads) k_form(const KArgs a) {
           for (int ii = 0; ii < 3; ++ii)
 #pragma unroll
             for (int jj = 0; jj < 3; ++jj) {
-              double v = 0.0;
+              T v = T(0);
 #pragma unroll
               for (int m = 0; m < 3; ++m)
 #pragma unroll
                 for (int n = 0; n < 3; ++n)
-                  v = fma(D[voigt_sel(ii, m) * 6 + voigt_sel(jj, n)], double(M[m][n]), v);
+                  v = fma(T(D[voigt_sel(ii, m) * 6 + voigt_sel(jj, n)]), M[m][n], v);
               V[ii][jj] = v;
             }
         }
@@ -472,6 +477,18 @@ __global__ void __launch_bounds__(kFormThreads) k_form(const KArgs a) {
         }
       }
 
+      if constexpr (GRAD) {
+        if (a.ke) {
+          // ---- block output for the row gather: the (pa <= pb) block, row-major
+          float *kb = a.ke + (static_cast<int64_t>(eb + e - a.e0) * NBLK + blk) * (NDN * NDN);
+#pragma unroll
+          for (int ii = 0; ii < NDN; ++ii)
+#pragma unroll
+            for (int jj = 0; jj < NDN; ++jj) kb[ii * NDN + jj] = float(V[ii][jj]);
+          continue;
+        }
+      }
+
       // ---- scatter (no atomics: one colour's elements share no node)
       const int32_t A = sConn[e * NNE + pa], B = sConn[e * NNE + pb];
       const int pAB = a.pos[(es * NNE + pa) * NNE + pb];
@@ -482,7 +499,7 @@ __global__ void __launch_bounds__(kFormThreads) k_form(const KArgs a) {
         for (int jj = 0; jj < NDN; ++jj) {
           const int64_t off = a.colperm ? a.colperm[a.cpoff[A] * NDN + NDN * pAB + jj]
                                         : static_cast<int64_t>(NDN * pAB + jj);
-          a.val[r0 + off] += V[ii][jj];
+          a.val[r0 + off] += double(V[ii][jj]);
         }
       }
       if (pa != pb) {
@@ -494,7 +511,7 @@ __global__ void __launch_bounds__(kFormThreads) k_form(const KArgs a) {
           for (int ii = 0; ii < NDN; ++ii) {
             const int64_t off = a.colperm ? a.colperm[a.cpoff[B] * NDN + NDN * pBA + ii]
                                           : static_cast<int64_t>(NDN * pBA + ii);
-            a.val[r0 + off] += Vt[jj][ii];
+            a.val[r0 + off] += double(Vt[jj][ii]);
           }
         }
       }

@@ -106,6 +106,7 @@ struct fegpu_femm {
   fegpu::DevBuf tab;                   // double: N[q][k], dN[q][k][m], w[q]
   fegpu::DevBuf xyz;                   // double [nnodes][4]
   bool has_geometry = false;
+  std::vector<int32_t> conn_host;      // element order, 0-based
 };
 
 struct fegpu_dofmap {
@@ -120,6 +121,18 @@ struct fegpu_dofmap {
   fegpu::DevBuf pos;        // uint16 [nelem][nne][nne], colour-sorted elements
   fegpu::DevBuf colperm;    // int32 per node block, only if !contiguous
   fegpu::DevBuf cpoff;      // int64 [nnodes], only if !contiguous
+  fegpu::DevBuf nptr;       // int64 [nnodes + 1]: node adjacency offsets
+  // row-gather plan (mixed precision), built on first use
+  bool gather_ready = false;
+  int64_t chunk = 0;        // elements per chunk of the block ring
+  int ring = 0;             // chunks held by the ring
+  std::vector<int64_t> chunk_nodes;  // gather node ranges per chunk
+  fegpu::DevBuf n2e_ptr;    // int64 [nnodes + 1]
+  fegpu::DevBuf n2e_elem;   // int32: incident elements, increasing
+  fegpu::DevBuf n2e_loc;    // uint8: local index of the node in that element
+  fegpu::DevBuf gnodes;     // int32: nodes in gather order
+  fegpu::DevBuf pos_orig;   // uint16 [nelem][nne][nne], element order
+  fegpu::DevBuf ke;         // float ring of element blocks
 };
 
 struct fegpu_matrix {
@@ -161,6 +174,7 @@ struct KArgs {
   double distort_tol;      // mixed path: det_min/det_max below -> FP64 geometry
   int64_t e0, e1;          // colour range of sorted elements
   int *status;             // device status word (0 = ok)
+  float *ke;               // block-output mode: element blocks of elements e0.. (or null)
 };
 
 // Launch one colour of one form.  Returns the number of kernel launches made.
@@ -175,6 +189,28 @@ int64_t greedy_element_coloring(int64_t nelem, int nne, const int32_t *conn0,
 
 // ---- pattern build on the device ------------------------------------------------
 void build_pattern(fegpu_dofmap *dm, const std::vector<int32_t> &hdof);
+
+// ---- row gather (mixed precision) ------------------------------------------------
+struct GArgs {
+  const int64_t *n2e_ptr;
+  const int32_t *n2e_elem;
+  const uint8_t *n2e_loc;
+  const int32_t *nodes;     // nodes in gather order
+  int64_t n0, n1;           // range of nodes[] handled by this launch
+  const int64_t *nptr;      // adjacency offsets (degree)
+  const uint16_t *pos;      // element-order slot maps
+  const float *ke;          // ring of element blocks
+  int64_t chunk;            // elements per ring chunk
+  int ring;                 // chunks in the ring
+  const int32_t *dof;
+  const int64_t *rowptr;
+  const int32_t *colperm;
+  const int64_t *cpoff;
+  double *val;
+  int maxdeg;
+};
+void build_gather_plan(fegpu_dofmap *dm, int nblk_values);
+int launch_gather(int etype, int ndn, const GArgs &g, int num_sms, cudaStream_t s);
 
 // ---- matrix utilities -----------------------------------------------------------
 void spmv(const fegpu_dofmap *dm, const double *val, const double *x, double *y,

@@ -74,15 +74,6 @@ __global__ void k_degree(const uint64_t *ukeys, const int64_t *nu, int32_t *deg,
   }
 }
 
-__global__ void k_rowlen(const int32_t *dof, int ndn, int64_t nnodes, const int32_t *deg,
-                         int64_t *rowlen) {
-  for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < nnodes;
-       n += (int64_t)gridDim.x * blockDim.x) {
-    if (deg[n] == 0) continue;
-    for (int i = 0; i < ndn; ++i) rowlen[dof[n * ndn + i]] = static_cast<int64_t>(ndn) * deg[n];
-  }
-}
-
 __global__ void k_contig(const int32_t *dof, int ndn, int64_t nnodes, const int32_t *deg,
                          int *flag) {
   for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < nnodes;
@@ -225,7 +216,8 @@ void build_pattern(fegpu_dofmap *dm, const std::vector<int32_t> &hdof) {
   FEGPU_CUDA(cudaStreamSynchronize(s));
   keys2.release();
 
-  DevBuf deg, nptr, nbr;
+  DevBuf deg, nbr;
+  DevBuf &nptr = dm->nptr;
   deg.alloc(sizeof(int32_t) * (N + 1));
   nptr.alloc(sizeof(int64_t) * (N + 1));
   nbr.alloc(sizeof(uint32_t) * (nu + 1));
@@ -303,7 +295,7 @@ void build_pattern(fegpu_dofmap *dm, const std::vector<int32_t> &hdof) {
     FEGPU_CUDA(cudaGetLastError());
     // cpoff[A] = nptr[A] * ndn: the kernels compute it from nptr
     dm->cpoff.alloc(sizeof(int64_t) * (N + 1));
-    FEGPU_CUDA(cudaMemcpyAsync(dm->cpoff.p, nptr.p, sizeof(int64_t) * (N + 1),
+    FEGPU_CUDA(cudaMemcpyAsync(dm->cpoff.p, dm->nptr.p, sizeof(int64_t) * (N + 1),
                                cudaMemcpyDeviceToDevice, s));
   }
 
