@@ -43,6 +43,17 @@ static int guarded(F &&f) {
 
 static void use_device(const fegpu_context *ctx) { FEGPU_CUDA(cudaSetDevice(ctx->device)); }
 
+int launch_mixed(int etype, int form, const KArgs &a, int num_sms, cudaStream_t s) {
+  switch (etype) {
+    case FEGPU_Q4: return launch_mixed_q4(form, a, num_sms, s);
+    case FEGPU_H8: return launch_mixed_h8(form, a, num_sms, s);
+    case FEGPU_H20: return launch_mixed_h20(form, a, num_sms, s);
+    case FEGPU_T4: return launch_mixed_t4(form, a, num_sms, s);
+    case FEGPU_T10: return launch_mixed_t10(form, a, num_sms, s);
+  }
+  throw Error{FEGPU_ERR_ARG, "unknown element type"};
+}
+
 int launch_form(int etype, int form, int precision, int ndn, const KArgs &a, int num_sms,
                 cudaStream_t s) {
   switch (etype) {
@@ -168,6 +179,7 @@ KArgs base_args(fegpu_matrix *K, fegpu_dofmap *dm) {
   a.conn = fm->conn.as<int32_t>();
   a.xyz = fm->xyz.as<double>();
   a.tab = fm->tab.as<double>();
+  a.tab32 = fm->tab32.as<float>();
   a.pos = dm->pos.as<uint16_t>();
   a.dof = dm->dof.as<int32_t>();
   a.rowptr = dm->rowptr.as<int64_t>();
@@ -213,13 +225,14 @@ void run_gather(fegpu_dofmap *dm, int form, KArgs &a) {
   const int bs = ndn * ndn, nblk = nne * (nne + 1) / 2;
   if (!dm->gather_ready) build_gather_plan(dm, nblk * bs);
   a.conn = fm->conn_orig.as<int32_t>();
-  a.te = choose_tile(fm->etype, form, FEGPU_MIXED, fm->npts);
-  const size_t smem = form_smem_bytes(fm->etype, form, FEGPU_MIXED, fm->npts, a.te);
-  FEGPU_REQUIRE(smem <= 227 * 1024, "quadrature rule too large for the element kernel");
+  a.te = mixed_tile(fm->etype, fm->npts);
+  FEGPU_REQUIRE(mixed_layout(nne, fm->mdim, fm->npts, a.te).total <= 227 * 1024,
+                "quadrature rule too large for the element kernel");
   GArgs g;
   g.n2e_ptr = dm->n2e_ptr.as<int64_t>();
   g.n2e_elem = dm->n2e_elem.as<int32_t>();
   g.n2e_loc = dm->n2e_loc.as<uint8_t>();
+  g.n2e_slot = dm->n2e_slot.as<int32_t>();
   g.nodes = dm->gnodes.as<int32_t>();
   g.nptr = dm->nptr.as<int64_t>();
   g.pos = dm->pos_orig.as<uint16_t>();
@@ -238,7 +251,7 @@ void run_gather(fegpu_dofmap *dm, int form, KArgs &a) {
     a.e0 = c * dm->chunk;
     a.e1 = std::min(fm->nelem, (c + 1) * dm->chunk);
     a.ke = dm->ke.as<float>() + (c % dm->ring) * dm->chunk * nblk * bs;
-    ctx->launches += launch_form(fm->etype, form, FEGPU_MIXED, ndn, a, ctx->num_sms, ctx->stream);
+    ctx->launches += launch_mixed(fm->etype, form, a, ctx->num_sms, ctx->stream);
     g.n0 = dm->chunk_nodes[c];
     g.n1 = dm->chunk_nodes[c + 1];
     ctx->launches += launch_gather(fm->etype, ndn, g, ctx->num_sms, ctx->stream);
@@ -417,6 +430,11 @@ int fegpu_femm_create(fegpu_context *ctx, int etype, int64_t nelem, const int64_
     std::memcpy(tab.data() + npts * nne * (mdim + 1), w, sizeof(double) * npts);
     fm->tab.alloc(sizeof(double) * tab.size());
     FEGPU_CUDA(cudaMemcpyAsync(fm->tab.p, tab.data(), sizeof(double) * tab.size(),
+                               cudaMemcpyHostToDevice, s));
+    std::vector<float> tab32(static_cast<size_t>(npts) * nne * mdim + npts);
+    for (size_t i = 0; i < tab32.size(); ++i) tab32[i] = static_cast<float>(tab[npts * nne + i]);
+    fm->tab32.alloc(sizeof(float) * tab32.size());
+    FEGPU_CUDA(cudaMemcpyAsync(fm->tab32.p, tab32.data(), sizeof(float) * tab32.size(),
                                cudaMemcpyHostToDevice, s));
     FEGPU_CUDA(cudaStreamSynchronize(s));
     *out = fm.release();

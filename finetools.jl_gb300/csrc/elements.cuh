@@ -46,7 +46,7 @@ template <> struct ElemT<FEGPU_T4> { static constexpr int NNE = 4, MDIM = 3; };
 template <> struct ElemT<FEGPU_T10> { static constexpr int NNE = 10, MDIM = 3; };
 
 struct SmemLayout {
-  size_t tab, X, G, WG, Jw, det, conn, pairs, total;
+  size_t tab, X, G, WG, Jw, det, conn, pairs, ftab, fx, total;
 };
 
 __host__ __device__ inline size_t align_up(size_t o, size_t a) { return (o + a - 1) / a * a; }
@@ -77,6 +77,13 @@ __host__ __device__ inline SmemLayout smem_layout(int nne, int mdim, int npts, i
   o += sizeof(int32_t) * te * nne;
   L.pairs = o;
   o += 2 * (nne * (nne + 1) / 2);
+  o = align_up(o, 16);
+  // FP32 copies for the mixed path: tables and element-relative coordinates
+  L.ftab = o;
+  if (tsize == 4) o += sizeof(float) * (npts * nne + npts * nne * mdim + npts);
+  o = align_up(o, 16);
+  L.fx = o;
+  if (tsize == 4) o += sizeof(float) * te * nne * 3;
   L.total = align_up(o, 16);
   return L;
 }
@@ -121,12 +128,13 @@ __device__ __forceinline__ C madd(C a, C b, C c) {  // c + a*b
 // (src/FESetModule.jl:426-435, 479-489) and gradN! (453-470, 507-544).
 // Writes the spatial gradients (as T) and returns the measure Jacobian
 // (times the other dimension when a two-manifold is integrated as a volume).
-template <int NNE, int MDIM, bool GRAD, typename C, typename T, bool EX = true>
-__device__ __forceinline__ C geometry_qp(const double *X, const double *dN, int sdim,
+template <int NNE, int MDIM, bool GRAD, typename C, typename T, bool EX = true, typename XT>
+__device__ __forceinline__ C geometry_qp(const XT *X, const XT *dN, int sdim,
                                          int measure_volume, double otherdim, T *g,
                                          float *det_out) {
-  // coordinates: absolute in FP64; relative to the first node in FP32 (the
-  // gradients of the basis sum to zero, so J is unchanged)
+  // coordinates: absolute in FP64; in FP32 relative to the element's first
+  // node (computed once per element: the gradients of the basis sum to zero,
+  // so J is unchanged)
   C J[3][MDIM];
 #pragma unroll
   for (int s = 0; s < 3; ++s)
@@ -136,8 +144,10 @@ __device__ __forceinline__ C geometry_qp(const double *X, const double *dN, int 
   for (int k = 0; k < NNE; ++k) {
     C x[3];
 #pragma unroll
-    for (int s = 0; s < 3; ++s)
-      x[s] = std::is_same<C, double>::value ? C(X[3 * k + s]) : C(X[3 * k + s] - X[s]);
+    for (int s = 0; s < 3; ++s) {
+      if constexpr (std::is_same<C, XT>::value) x[s] = X[3 * k + s];
+      else x[s] = C(X[3 * k + s] - X[s]);  // FP64 recompute from absolute coordinates
+    }
 #pragma unroll
     for (int m = 0; m < MDIM; ++m) {
       const C d = C(dN[k * MDIM + m]);
@@ -262,9 +272,14 @@ __global__ void __launch_bounds__(kFormThreads) k_form(const KArgs a) {
   float *sDet = reinterpret_cast<float *>(smem + L.det);
   int32_t *sConn = reinterpret_cast<int32_t *>(smem + L.conn);
   uint8_t *sPair = smem + L.pairs;
+  float *fdN = reinterpret_cast<float *>(smem + L.ftab) + npts * NNE;  // FP32 dN (mixed)
+  float *fX = reinterpret_cast<float *>(smem + L.fx);                 // FP32 relative coords
   const int tid = threadIdx.x, nth = blockDim.x;
 
-  for (int i = tid; i < npts * NNE * (MDIM + 1) + npts; i += nth) sN[i] = a.tab[i];
+  for (int i = tid; i < npts * NNE * (MDIM + 1) + npts; i += nth) {
+    sN[i] = a.tab[i];
+    if constexpr (MIXED) reinterpret_cast<float *>(smem + L.ftab)[i] = float(a.tab[i]);
+  }
   for (int i = tid; i < NBLK; i += nth) {
     int r = i, pa = 0;
     while (r >= NNE - pa) {
@@ -291,15 +306,28 @@ __global__ void __launch_bounds__(kFormThreads) k_form(const KArgs a) {
       sX[3 * i + 2] = p[2];
     }
     __syncthreads();
+    if constexpr (MIXED) {
+      for (int i = tid; i < ne * NNE * 3; i += nth) {
+        const int e = i / (NNE * 3), r = i - e * NNE * 3;
+        fX[i] = float(sX[i] - sX[e * NNE * 3 + r % 3]);
+      }
+      __syncthreads();
+    }
 
     // ---- geometry per (element, quadrature point)
     for (int i = tid; i < ne * npts; i += nth) {
       const int e = i / npts, q = i - e * npts;
       T *g = sG + (static_cast<size_t>(e) * npts + q) * NNE * MDIM;
       T *wg = sWG + (static_cast<size_t>(e) * npts + q) * NNE * MDIM;
-      const T Jac = T(geometry_qp<NNE, MDIM, GRAD, T, T, EXACT>(sX + e * NNE * 3, sdN + q * NNE * MDIM,
-                                                         a.sdim, vol, a.otherdim, g,
-                                                         sDet + e * npts + q));
+      T Jac;
+      if constexpr (MIXED)
+        Jac = geometry_qp<NNE, MDIM, GRAD, float, T, EXACT>(fX + e * NNE * 3, fdN + q * NNE * MDIM,
+                                                          a.sdim, vol, a.otherdim, g,
+                                                          sDet + e * npts + q);
+      else
+        Jac = geometry_qp<NNE, MDIM, GRAD, double, T, EXACT>(sX + e * NNE * 3, sdN + q * NNE * MDIM,
+                                                           a.sdim, vol, a.otherdim, g,
+                                                           sDet + e * npts + q);
       qp_weights<NNE, MDIM, FORM, T>(a, eb + e, q, npts, Jac, sw[q], g, wg, sJw + e * npts + q);
     }
     if constexpr (MIXED) {

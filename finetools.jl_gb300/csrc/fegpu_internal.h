@@ -104,6 +104,7 @@ struct fegpu_femm {
   fegpu::DevBuf conn;                  // int32 nelem x nne, colour-sorted
   fegpu::DevBuf perm;                  // int32 sorted position -> element
   fegpu::DevBuf tab;                   // double: N[q][k], dN[q][k][m], w[q]
+  fegpu::DevBuf tab32;                 // float: dN[q][k][m], w[q]
   fegpu::DevBuf xyz;                   // double [nnodes][4]
   bool has_geometry = false;
   std::vector<int32_t> conn_host;      // element order, 0-based
@@ -130,6 +131,7 @@ struct fegpu_dofmap {
   fegpu::DevBuf n2e_ptr;    // int64 [nnodes + 1]
   fegpu::DevBuf n2e_elem;   // int32: incident elements, increasing
   fegpu::DevBuf n2e_loc;    // uint8: local index of the node in that element
+  fegpu::DevBuf n2e_slot;   // int32: block-ring slot of that element
   fegpu::DevBuf gnodes;     // int32: nodes in gather order
   fegpu::DevBuf pos_orig;   // uint16 [nelem][nne][nne], element order
   fegpu::DevBuf ke;         // float ring of element blocks
@@ -157,6 +159,7 @@ struct KArgs {
   const int32_t *conn;     // colour-sorted nelem x nne
   const double *xyz;       // [nnodes][4]
   const double *tab;       // N, dN, w tables
+  const float *tab32;      // FP32 dN and w tables (mixed path)
   const uint16_t *pos;     // colour-sorted nelem x nne x nne
   const int32_t *dof;      // [nnodes][ndn]
   const int64_t *rowptr;   // CSR rows
@@ -195,6 +198,7 @@ struct GArgs {
   const int64_t *n2e_ptr;
   const int32_t *n2e_elem;
   const uint8_t *n2e_loc;
+  const int32_t *n2e_slot;  // ring slot of each incident element
   const int32_t *nodes;     // nodes in gather order
   int64_t n0, n1;           // range of nodes[] handled by this launch
   const int64_t *nptr;      // adjacency offsets (degree)

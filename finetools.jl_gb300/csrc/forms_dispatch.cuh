@@ -4,29 +4,24 @@
 #pragma once
 
 #include "elements.cuh"
+#include "mixed.cuh"
 
 namespace fegpu {
 
+// FP64 colour-ordered kernels (every form).  The mixed-precision path goes
+// through launch_mixed_et (FP32 element blocks for the row gather).
 template <int ET>
 int launch_form_et(int form, int precision, int ndn, const KArgs &a, int sms, cudaStream_t s) {
   constexpr bool SOLID = ElemT<ET>::MDIM == 3;
-  const bool mixed = precision == FEGPU_MIXED;
+  (void)precision;
   switch (form) {
-    case F_DIFF_ISO:
-      return mixed ? launch_one<ET, F_DIFF_ISO, float, 1>(a, sms, s)
-                   : launch_one<ET, F_DIFF_ISO, double, 1>(a, sms, s);
-    case F_DIFF_GEN:
-      return mixed ? launch_one<ET, F_DIFF_GEN, float, 1>(a, sms, s)
-                   : launch_one<ET, F_DIFF_GEN, double, 1>(a, sms, s);
+    case F_DIFF_ISO: return launch_one<ET, F_DIFF_ISO, double, 1>(a, sms, s);
+    case F_DIFF_GEN: return launch_one<ET, F_DIFF_GEN, double, 1>(a, sms, s);
     case F_ELAST_ISO:
-      if constexpr (SOLID)
-        return mixed ? launch_one<ET, F_ELAST_ISO, float, 3>(a, sms, s)
-                     : launch_one<ET, F_ELAST_ISO, double, 3>(a, sms, s);
+      if constexpr (SOLID) return launch_one<ET, F_ELAST_ISO, double, 3>(a, sms, s);
       break;
     case F_ELAST_GEN:
-      if constexpr (SOLID)
-        return mixed ? launch_one<ET, F_ELAST_GEN, float, 3>(a, sms, s)
-                     : launch_one<ET, F_ELAST_GEN, double, 3>(a, sms, s);
+      if constexpr (SOLID) return launch_one<ET, F_ELAST_GEN, double, 3>(a, sms, s);
       break;
     case F_DOT:
       if (ndn == 1) return launch_one<ET, F_DOT, double, 1>(a, sms, s);
@@ -42,10 +37,32 @@ int launch_form_et(int form, int precision, int ndn, const KArgs &a, int sms, cu
   throw Error{FEGPU_ERR_ARG, "form not available for this element type / DOF count"};
 }
 
+template <int ET>
+int launch_mixed_et(int form, const KArgs &a, int sms, cudaStream_t s) {
+  constexpr bool SOLID = ElemT<ET>::MDIM == 3;
+  switch (form) {
+    case F_DIFF_ISO: return launch_blocks_mixed_t<ET, F_DIFF_ISO, 1>(a, sms, s);
+    case F_DIFF_GEN: return launch_blocks_mixed_t<ET, F_DIFF_GEN, 1>(a, sms, s);
+    case F_ELAST_ISO:
+      if constexpr (SOLID) return launch_blocks_mixed_t<ET, F_ELAST_ISO, 3>(a, sms, s);
+      break;
+    case F_ELAST_GEN:
+      if constexpr (SOLID) return launch_blocks_mixed_t<ET, F_ELAST_GEN, 3>(a, sms, s);
+      break;
+  }
+  throw Error{FEGPU_ERR_ARG, "mixed precision: form not available for this element type"};
+}
+
 int launch_form_q4(int, int, int, const KArgs &, int, cudaStream_t);
 int launch_form_h8(int, int, int, const KArgs &, int, cudaStream_t);
 int launch_form_h20(int, int, int, const KArgs &, int, cudaStream_t);
 int launch_form_t4(int, int, int, const KArgs &, int, cudaStream_t);
 int launch_form_t10(int, int, int, const KArgs &, int, cudaStream_t);
+int launch_mixed(int etype, int form, const KArgs &a, int sms, cudaStream_t s);
+int launch_mixed_q4(int, const KArgs &, int, cudaStream_t);
+int launch_mixed_h8(int, const KArgs &, int, cudaStream_t);
+int launch_mixed_h20(int, const KArgs &, int, cudaStream_t);
+int launch_mixed_t4(int, const KArgs &, int, cudaStream_t);
+int launch_mixed_t10(int, const KArgs &, int, cudaStream_t);
 
 }  // namespace fegpu

@@ -1,8 +1,11 @@
-// Element kernels for FEGPU_H20 (all forms, both precisions).
+// Element kernels for FEGPU_H20: FP64 colour kernels and FP32 block kernels.
 #include "forms_dispatch.cuh"
 
 namespace fegpu {
 int launch_form_h20(int form, int precision, int ndn, const KArgs &a, int sms, cudaStream_t s) {
   return launch_form_et<FEGPU_H20>(form, precision, ndn, a, sms, s);
+}
+int launch_mixed_h20(int form, const KArgs &a, int sms, cudaStream_t s) {
+  return launch_mixed_et<FEGPU_H20>(form, a, sms, s);
 }
 }  // namespace fegpu

@@ -24,6 +24,13 @@ namespace {
 
 constexpr int kWarpsPerCta = 8;
 
+// floats of shared memory per warp: hi and lo accumulators of the node's
+// NDN rows, rounded up to a multiple of four
+__host__ __device__ inline int gather_warp_stride(int ndn, int maxdeg) {
+  const int n = 2 * ndn * maxdeg * ndn;
+  return (n + 3) / 4 * 4;
+}
+
 // Error-free accumulation of v into (h, l): two-sum (Knuth).
 __device__ __forceinline__ void two_sum_acc(float &h, float &l, float v) {
   const float s = __fadd_rn(h, v);
@@ -44,10 +51,14 @@ __device__ __forceinline__ double ff_to_double(float h, float l) {
   h = s;
   const uint32_t hb = __float_as_uint(h);
   const uint32_t eh = (hb >> 23) & 0xffu;
-  if (eh == 0u || eh == 0xffu) {
-    // zero, subnormal, inf or nan: not produced by finite element blocks of
-    // normal magnitude; the plain conversion keeps the value
-    return static_cast<double>(h) + static_cast<double>(l);
+  if (eh == 0u) {
+    // zero (or an FP32-subnormal sum, below 1.2e-38): signed zero
+    return __longlong_as_double(static_cast<long long>(static_cast<uint64_t>(hb >> 31) << 63));
+  }
+  if (eh == 0xffu) {  // inf / nan keep their class
+    const uint64_t nanbit = (hb & 0x7fffffu) ? (1ull << 51) : 0ull;
+    return __longlong_as_double(static_cast<long long>(
+        (static_cast<uint64_t>(hb >> 31) << 63) | (0x7ffull << 52) | nanbit));
   }
   const uint64_t mh = static_cast<uint64_t>((hb & 0x7fffffu) | 0x800000u);
   uint64_t H = mh << 37;
@@ -83,26 +94,29 @@ template <int NNE, int NDN>
 __global__ void __launch_bounds__(kWarpsPerCta * 32) k_gather(const GArgs g) {
   constexpr int NBLK = NNE * (NNE + 1) / 2;
   constexpr int BS = NDN * NDN;
-  extern __shared__ float gsm[];
+  extern __shared__ __align__(16) float gsm[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int cmax = g.maxdeg * NDN;
-  float *hi = gsm + static_cast<size_t>(warp) * 2 * NDN * cmax;
+  // per-warp region padded to a multiple of 4 floats: every warp's region
+  // starts on a 16-byte boundary (the zeroing below stores float4)
+  const int wstride = gather_warp_stride(NDN, g.maxdeg);
+  float *hi = gsm + static_cast<size_t>(warp) * wstride;
   float *lo = hi + NDN * cmax;
   for (int64_t t = g.n0 + static_cast<int64_t>(blockIdx.x) * kWarpsPerCta + warp; t < g.n1;
        t += static_cast<int64_t>(gridDim.x) * kWarpsPerCta) {
     const int32_t A = g.nodes[t];
     const int cols = static_cast<int>(g.nptr[A + 1] - g.nptr[A]) * NDN;
-    for (int c = lane; c < NDN * cmax; c += 32) {
-      hi[c] = 0.f;
-      lo[c] = 0.f;
+    {
+      float4 *z = reinterpret_cast<float4 *>(hi);  // hi and lo are contiguous
+      const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+      for (int c = lane; c < (2 * NDN * cmax) / 4; c += 32) z[c] = zero;
+      for (int c = ((2 * NDN * cmax) / 4) * 4 + lane; c < 2 * NDN * cmax; c += 32) hi[c] = 0.f;
     }
     __syncwarp();
     for (int64_t q = g.n2e_ptr[A]; q < g.n2e_ptr[A + 1]; ++q) {
       const int64_t e = g.n2e_elem[q];
       const int a = g.n2e_loc[q];
-      const int64_t ce = e / g.chunk;
-      const int64_t slot = (ce % g.ring) * g.chunk + (e - ce * g.chunk);
-      const float *kb = g.ke + slot * NBLK * BS;
+      const float *kb = g.ke + static_cast<int64_t>(g.n2e_slot[q]) * NBLK * BS;
       const uint16_t *pe = g.pos + (e * NNE + a) * NNE;
       for (int task = lane; task < NNE * NDN; task += 32) {
         const int b = task / NDN, j = task - (task / NDN) * NDN;
@@ -135,7 +149,7 @@ template <int NNE, int NDN>
 int launch_t(const GArgs &g, int num_sms, cudaStream_t s) {
   const int64_t n = g.n1 - g.n0;
   if (n <= 0) return 0;
-  const size_t smem = sizeof(float) * 2 * NDN * static_cast<size_t>(g.maxdeg) * NDN * kWarpsPerCta;
+  const size_t smem = sizeof(float) * static_cast<size_t>(gather_warp_stride(NDN, g.maxdeg)) * kWarpsPerCta;
   FEGPU_REQUIRE(smem <= 227 * 1024, "node degree too large for the row gather");
   auto kern = k_gather<NNE, NDN>;
   FEGPU_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -199,6 +213,7 @@ void build_gather_plan(fegpu_dofmap *dm, int block_values) {
       elem[q] = static_cast<int32_t>(e);
       loc[q] = static_cast<uint8_t>(a);
     }
+  std::vector<int32_t> slot(elem.size());
   // a node is gathered after the chunk of its last element
   std::vector<int64_t> cnt(nch + 1, 0);
   int64_t span = 0;
@@ -217,6 +232,14 @@ void build_gather_plan(fegpu_dofmap *dm, int block_values) {
     order[at[elem[ptr[n + 1] - 1] / dm->chunk]++] = static_cast<int32_t>(n);
   }
   dm->ring = static_cast<int>(std::min<int64_t>(span + 1, nch));
+  for (size_t q = 0; q < elem.size(); ++q) {
+    const int64_t ce = elem[q] / dm->chunk;
+    slot[q] = static_cast<int32_t>((ce % dm->ring) * dm->chunk + (elem[q] - ce * dm->chunk));
+  }
+  dm->n2e_slot.alloc(sizeof(int32_t) * std::max<size_t>(slot.size(), 1));
+  if (!slot.empty())
+    FEGPU_CUDA(cudaMemcpyAsync(dm->n2e_slot.p, slot.data(), sizeof(int32_t) * slot.size(),
+                               cudaMemcpyHostToDevice, s));
   dm->n2e_ptr.alloc(sizeof(int64_t) * (N + 1));
   dm->n2e_elem.alloc(sizeof(int32_t) * elem.size());
   dm->n2e_loc.alloc(loc.size());

@@ -1,0 +1,408 @@
+// FP32 element-block kernel of the mixed-precision path.
+//
+// For a range of elements (one chunk, element order) it writes the upper
+// node-pair blocks of every element matrix, in FP32, to the block ring read
+// by the row gather (gather.cu).  Per tile of TE elements:
+//   A. connectivity; coordinates relative to the element's first node, in
+//      FP32 (the basis gradients sum to zero, so J is unchanged);
+//   B. one thread per (element, point): J = X' dN (locjac!), det J and J^-1
+//      in FP32; an element whose det_min / det_max over its points is below
+//      the distortion threshold gets its J, det J and J^-1 recomputed in FP64
+//      from the absolute coordinates (the only FP64 arithmetic of the path);
+//   C. one thread per (element, point, node): g = dN J^-1 and the weighted
+//      gradient w g (w = det J * weight, times the scalar conductivity or
+//      kappa for diffusion), stored as float4 so a point costs one 16-byte
+//      shared load per node;
+//   D. one thread per (element, node a, group of up to four nodes b >= a):
+//      the Gram sums M^{mn}_{ab} = sum_q (w g_am)(g_bn) for four blocks at
+//      once (w g_a is loaded once and broadcast across the warp), the
+//      coefficient map of the form (isotropic Lame, general D, kappa), and
+//      the FP32 block store.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <type_traits>
+
+#include "elements.cuh"
+
+namespace fegpu {
+
+constexpr int kMixedThreads = 256;
+
+struct MixedLayout {
+  size_t conn, fx, jac, jinv, jw, det, lame, g, wg, total;
+};
+
+__host__ __device__ inline MixedLayout mixed_layout(int nne, int mdim, int npts, int te) {
+  MixedLayout L;
+  size_t o = 0;
+  L.conn = o;
+  o += sizeof(int32_t) * te * nne;
+  o = align_up(o, 16);
+  L.fx = o;
+  o += sizeof(float) * te * nne * 3;
+  o = align_up(o, 16);
+  L.jac = o;
+  o += sizeof(float) * te * npts * 9;
+  L.jinv = o;
+  o += sizeof(float) * te * npts * 9;
+  L.lame = o;
+  o += sizeof(float) * te * 2;
+  L.jw = o;
+  o += sizeof(float) * te * npts;
+  L.det = o;
+  o += sizeof(float) * te * npts;
+  o = align_up(o, 16);
+  L.g = o;
+  o += sizeof(float4) * te * npts * nne;
+  L.wg = o;
+  o += sizeof(float4) * te * npts * nne;
+  L.total = align_up(o, 16);
+  return L;
+}
+
+// number of (a, group of <= 4 nodes b >= a) tasks of one element
+__host__ __device__ constexpr int mixed_groups(int nne) {
+  int n = 0;
+  for (int a = 0; a < nne; ++a) n += (nne - a + 3) / 4;
+  return n;
+}
+
+// FP64 Jacobian, determinant and inverse of one point (distorted elements).
+template <int NNE, int MDIM>
+__device__ void jacobian_fp64(const double *xyz, const int32_t *conn, const double *dN, int sdim,
+                              double *inv, double &det) {
+  double J[3][MDIM];
+#pragma unroll
+  for (int s = 0; s < 3; ++s)
+#pragma unroll
+    for (int m = 0; m < MDIM; ++m) J[s][m] = 0.0;
+  for (int k = 0; k < NNE; ++k) {
+    const double *p = xyz + 4 * static_cast<int64_t>(conn[k]);
+#pragma unroll
+    for (int m = 0; m < MDIM; ++m) {
+      const double d = dN[k * MDIM + m];
+#pragma unroll
+      for (int s = 0; s < 3; ++s) J[s][m] = fma(p[s], d, J[s][m]);
+    }
+  }
+  if constexpr (MDIM == 3) {
+    const double c0 = J[1][1] * J[2][2] - J[2][1] * J[1][2];
+    const double c1 = J[1][0] * J[2][2] - J[1][2] * J[2][0];
+    const double c2 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+    det = J[0][0] * c0 - J[0][1] * c1 + J[0][2] * c2;
+    const double id = 1.0 / det;
+    inv[0] = c0 * id;
+    inv[1] = -(J[0][1] * J[2][2] - J[0][2] * J[2][1]) * id;
+    inv[2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
+    inv[3] = -c1 * id;
+    inv[4] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
+    inv[5] = -(J[0][0] * J[1][2] - J[1][0] * J[0][2]) * id;
+    inv[6] = (J[1][0] * J[2][1] - J[2][0] * J[1][1]) * id;
+    inv[7] = -(J[0][0] * J[2][1] - J[2][0] * J[0][1]) * id;
+    inv[8] = (J[0][0] * J[1][1] - J[1][0] * J[0][1]) * id;
+  } else {
+    det = J[0][0] * J[1][1] - J[1][0] * J[0][1];
+    const double id = 1.0 / det;
+    inv[0] = J[1][1] * id;
+    inv[1] = -J[0][1] * id;
+    inv[3] = -J[1][0] * id;
+    inv[4] = J[0][0] * id;
+    (void)sdim;
+  }
+}
+
+template <int ET, int FORM, int NDN>
+__global__ void __launch_bounds__(kMixedThreads) k_blocks_mixed(const KArgs a) {
+  constexpr int NNE = ElemT<ET>::NNE, MDIM = ElemT<ET>::MDIM;
+  constexpr int NBLK = NNE * (NNE + 1) / 2;
+  constexpr int NGRP = mixed_groups(NNE);
+  constexpr int BS = NDN * NDN;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int npts = a.npts, te = a.te;
+  const MixedLayout L = mixed_layout(NNE, MDIM, npts, te);
+  // FP32 tables live in global memory (read through L1): dN[q][k][m], then w[q]
+  const float *fdN = a.tab32;
+  const float *fw = a.tab32 + npts * NNE * MDIM;
+  float *sJ = reinterpret_cast<float *>(smem + L.jac);
+  float *sLame = reinterpret_cast<float *>(smem + L.lame);
+  int32_t *sConn = reinterpret_cast<int32_t *>(smem + L.conn);
+  float *fX = reinterpret_cast<float *>(smem + L.fx);
+  float *sJinv = reinterpret_cast<float *>(smem + L.jinv);
+  float *sJw = reinterpret_cast<float *>(smem + L.jw);
+  float *sDet = reinterpret_cast<float *>(smem + L.det);
+  float4 *sG = reinterpret_cast<float4 *>(smem + L.g);
+  float4 *sWG = reinterpret_cast<float4 *>(smem + L.wg);
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const double *tabdN = a.tab + npts * NNE;
+  const float tol = static_cast<float>(a.distort_tol);
+  const float odim = static_cast<float>(a.otherdim);
+  const int64_t nel = a.e1 - a.e0;
+  const int64_t ntiles = (nel + te - 1) / te;
+
+  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int64_t eb = a.e0 + tile * te;
+    const int ne = static_cast<int>(min(static_cast<int64_t>(te), a.e1 - eb));
+    __syncthreads();
+    for (int i = tid; i < ne * NNE; i += nth) sConn[i] = a.conn[eb * NNE + i];
+    __syncthreads();
+    // A. FP32 coordinates relative to the first node
+    for (int i = tid; i < ne * NNE; i += nth) {
+      const int e = i / NNE;
+      const double *p = a.xyz + 4 * static_cast<int64_t>(sConn[i]);
+      const double *p0 = a.xyz + 4 * static_cast<int64_t>(sConn[e * NNE]);
+#pragma unroll
+      for (int s = 0; s < 3; ++s) fX[3 * i + s] = float(p[s] - p0[s]);
+    }
+    if constexpr (FORM == F_ELAST_ISO) {
+      for (int e = tid; e < ne; e += nth) {
+        if (a.coef_kind == FEGPU_COEF_ISO_LAME) {
+          sLame[2 * e] = float(a.coef[2 * (eb + e)]);
+          sLame[2 * e + 1] = float(a.coef[2 * (eb + e) + 1]);
+        } else {
+          sLame[2 * e] = float(a.cconst[0]);
+          sLame[2 * e + 1] = float(a.cconst[1]);
+        }
+      }
+    }
+    __syncthreads();
+    // B1. rows of J = X' dN per (element, point, space direction)
+    for (int i = tid; i < ne * npts * 3; i += nth) {
+      const int eq = i / 3, s = i - eq * 3;
+      const int e = eq / npts, q = eq - e * npts;
+      const float *X = fX + e * NNE * 3 + s;
+      const float *d = fdN + q * NNE * MDIM;
+      float r[MDIM];
+#pragma unroll
+      for (int m = 0; m < MDIM; ++m) r[m] = 0.f;
+#pragma unroll
+      for (int k = 0; k < NNE; ++k)
+#pragma unroll
+        for (int m = 0; m < MDIM; ++m) r[m] = fmaf(X[3 * k], d[k * MDIM + m], r[m]);
+#pragma unroll
+      for (int m = 0; m < MDIM; ++m) sJ[eq * 9 + s * 3 + m] = r[m];
+    }
+    __syncthreads();
+    // B2. det J and J^-1 per (element, point) in FP32
+    for (int i = tid; i < ne * npts; i += nth) {
+      float J[3][MDIM];
+#pragma unroll
+      for (int s = 0; s < 3; ++s)
+#pragma unroll
+        for (int m = 0; m < MDIM; ++m) J[s][m] = sJ[i * 9 + s * 3 + m];
+      float *inv = sJinv + i * 9;
+      float det;
+      if constexpr (MDIM == 3) {
+        const float c0 = J[1][1] * J[2][2] - J[2][1] * J[1][2];
+        const float c1 = J[1][0] * J[2][2] - J[1][2] * J[2][0];
+        const float c2 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+        det = J[0][0] * c0 - J[0][1] * c1 + J[0][2] * c2;
+        const float id = 1.f / det;
+        inv[0] = c0 * id;
+        inv[1] = -(J[0][1] * J[2][2] - J[0][2] * J[2][1]) * id;
+        inv[2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
+        inv[3] = -c1 * id;
+        inv[4] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
+        inv[5] = -(J[0][0] * J[1][2] - J[1][0] * J[0][2]) * id;
+        inv[6] = (J[1][0] * J[2][1] - J[2][0] * J[1][1]) * id;
+        inv[7] = -(J[0][0] * J[2][1] - J[2][0] * J[0][1]) * id;
+        inv[8] = (J[0][0] * J[1][1] - J[1][0] * J[0][1]) * id;
+      } else {
+        det = J[0][0] * J[1][1] - J[1][0] * J[0][1];
+        const float id = 1.f / det;
+        inv[0] = J[1][1] * id;
+        inv[1] = -J[0][1] * id;
+        inv[3] = -J[1][0] * id;
+        inv[4] = J[0][0] * id;
+      }
+      sDet[i] = det;
+    }
+    __syncthreads();
+    // B'. distorted elements: FP64 Jacobian; then the point weight
+    for (int i = tid; i < ne * npts; i += nth) {
+      const int e = i / npts, q = i - e * npts;
+      float dmin = 3.0e38f, dmax = 0.f;
+      for (int r = 0; r < npts; ++r) {
+        const float v = fabsf(sDet[e * npts + r]);
+        dmin = fminf(dmin, v);
+        dmax = fmaxf(dmax, v);
+      }
+      float det = sDet[i];
+      if (!(dmin > tol * dmax)) {
+        double inv[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, dd;
+        jacobian_fp64<NNE, MDIM>(a.xyz, sConn + e * NNE, tabdN + q * NNE * MDIM, a.sdim, inv, dd);
+#pragma unroll
+        for (int r = 0; r < 9; ++r) sJinv[i * 9 + r] = float(inv[r]);
+        det = float(dd);
+      }
+      float w = det * fw[q];
+      if (MDIM == 2) w *= odim;
+      if constexpr (FORM == F_DIFF_ISO) {
+        float c = 1.f;
+        if (a.coef_kind == FEGPU_COEF_CONST) c = float(a.cconst[0]);
+        else if (a.coef_kind == FEGPU_COEF_PER_ELEMENT) c = float(a.coef[eb + e]);
+        else if (a.coef_kind == FEGPU_COEF_PER_QP) c = float(a.coef[(eb + e) * npts + q]);
+        w *= c;
+      }
+      sJw[i] = w;
+    }
+    __syncthreads();
+    // C. gradients and weighted gradients per (element, point, node)
+    for (int i = tid; i < ne * npts * NNE; i += nth) {
+      const int eq = i / NNE, k = i - eq * NNE;
+      const int q = eq - (eq / npts) * npts;
+      const float *inv = sJinv + eq * 9;
+      const float *d = fdN + (q * NNE + k) * MDIM;
+      float g[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+      for (int c = 0; c < MDIM; ++c) {
+        float v = 0.f;
+#pragma unroll
+        for (int m = 0; m < MDIM; ++m) v = fmaf(d[m], inv[m * 3 + c], v);
+        g[c] = v;
+      }
+      const float w = sJw[eq];
+      float4 wg = make_float4(w * g[0], w * g[1], w * g[2], 0.f);
+      if constexpr (FORM == F_DIFF_GEN) {
+        const int e = eq / npts;
+        const double *kap = a.coef_kind == FEGPU_COEF_PER_ELEMENT
+                                ? a.coef + (eb + e) * MDIM * MDIM : a.cconst;
+        float kg[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+        for (int m = 0; m < MDIM; ++m)
+#pragma unroll
+          for (int p = 0; p < MDIM; ++p) kg[m] = fmaf(float(kap[m * MDIM + p]), g[p], kg[m]);
+        wg = make_float4(w * kg[0], w * kg[1], w * kg[2], 0.f);
+      }
+      sG[i] = make_float4(g[0], g[1], g[2], 0.f);
+      sWG[i] = wg;
+    }
+    __syncthreads();
+    // D. Gram sums for (a, up to four b >= a), coefficient map, block store
+    for (int i = tid; i < ne * NGRP; i += nth) {
+      const int e = i / NGRP;
+      int r = i - e * NGRP, pa = 0;
+      while (r >= (NNE - pa + 3) / 4) {
+        r -= (NNE - pa + 3) / 4;
+        ++pa;
+      }
+      const int b0 = pa + 4 * r;
+      const int nb = min(4, NNE - b0);
+      float M[4][3][3];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int m = 0; m < 3; ++m)
+#pragma unroll
+          for (int n = 0; n < 3; ++n) M[u][m][n] = 0.f;
+      const float4 *wa = sWG + (e * npts) * NNE + pa;
+      const float4 *gb = sG + (e * npts) * NNE + b0;
+      for (int q = 0; q < npts; ++q) {
+        const float4 x = wa[q * NNE];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          if (u < nb) {
+            const float4 y = gb[q * NNE + u];
+            if constexpr (FORM == F_DIFF_ISO || FORM == F_DIFF_GEN) {
+              M[u][0][0] = fmaf(x.x, y.x, fmaf(x.y, y.y, fmaf(x.z, y.z, M[u][0][0])));
+            } else {
+              const float xs[3] = {x.x, x.y, x.z}, ys[3] = {y.x, y.y, y.z};
+#pragma unroll
+              for (int m = 0; m < 3; ++m)
+#pragma unroll
+                for (int n = 0; n < 3; ++n) M[u][m][n] = fmaf(xs[m], ys[n], M[u][m][n]);
+            }
+          }
+        }
+      }
+      const int64_t es = eb + e;
+      float lam = 0.f, mu = 0.f;
+      if constexpr (FORM == F_ELAST_ISO) {
+        lam = sLame[2 * e];
+        mu = sLame[2 * e + 1];
+      }
+      const double *D = (FORM == F_ELAST_GEN && a.coef_kind == FEGPU_COEF_PER_ELEMENT)
+                             ? a.coef + es * 36 : a.cconst;
+      float *kb = a.ke + static_cast<int64_t>(eb + e - a.e0) * NBLK * BS;
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        if (u >= nb) break;
+        const int pb = b0 + u;
+        float *out = kb + (pa * NNE - pa * (pa - 1) / 2 + (pb - pa)) * BS;
+        if constexpr (FORM == F_DIFF_ISO || FORM == F_DIFF_GEN) {
+          out[0] = M[u][0][0];
+        } else {
+          float V[3][3];
+          if constexpr (FORM == F_ELAST_ISO) {
+            const float mtr = mu * (M[u][0][0] + M[u][1][1] + M[u][2][2]);
+#pragma unroll
+            for (int ii = 0; ii < 3; ++ii)
+#pragma unroll
+              for (int jj = 0; jj < 3; ++jj)
+                V[ii][jj] = fmaf(lam, M[u][ii][jj], mu * M[u][jj][ii]) + (ii == jj ? mtr : 0.f);
+          } else {
+#pragma unroll
+            for (int ii = 0; ii < 3; ++ii)
+#pragma unroll
+              for (int jj = 0; jj < 3; ++jj) {
+                float v = 0.f;
+#pragma unroll
+                for (int m = 0; m < 3; ++m)
+#pragma unroll
+                  for (int n = 0; n < 3; ++n)
+                    v = fmaf(float(D[voigt_sel(ii, m) * 6 + voigt_sel(jj, n)]), M[u][m][n], v);
+                V[ii][jj] = v;
+              }
+          }
+          if (pb == pa) {
+#pragma unroll
+            for (int ii = 0; ii < 3; ++ii)
+#pragma unroll
+              for (int jj = 0; jj < ii; ++jj) V[ii][jj] = V[jj][ii];
+          }
+#pragma unroll
+          for (int ii = 0; ii < 3; ++ii)
+#pragma unroll
+            for (int jj = 0; jj < 3; ++jj) out[ii * 3 + jj] = V[ii][jj];
+        }
+      }
+    }
+  }
+}
+
+// Elements per tile: enough Gram tasks for two passes of the CTA, within a
+// shared-memory budget that leaves two CTAs per SM.
+inline int mixed_tile(int etype, int npts) {
+  const int nne = nodes_per_elem(etype), mdim = manif_dim(etype);
+  const size_t budget = 72 * 1024;
+  const MixedLayout one = mixed_layout(nne, mdim, npts, 1);
+  const MixedLayout two = mixed_layout(nne, mdim, npts, 2);
+  const size_t per = two.total - one.total;
+  const size_t fixed = one.total - per;
+  const int fit = static_cast<int>((budget - std::min(budget, fixed)) / per);
+  const int want = (kMixedThreads + mixed_groups(nne) - 1) / mixed_groups(nne);
+  return std::max(1, std::min(fit, want));
+}
+
+template <int ET, int FORM, int NDN>
+int launch_blocks_mixed_t(const KArgs &a, int num_sms, cudaStream_t s) {
+  constexpr int NNE = ElemT<ET>::NNE, MDIM = ElemT<ET>::MDIM;
+  const MixedLayout L = mixed_layout(NNE, MDIM, a.npts, a.te);
+  auto kern = k_blocks_mixed<ET, FORM, NDN>;
+  FEGPU_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  static_cast<int>(L.total)));
+  int per_sm = 0;
+  FEGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kMixedThreads, L.total));
+  per_sm = std::max(per_sm, 1);
+  const int64_t nel = a.e1 - a.e0;
+  if (nel <= 0) return 0;
+  const int64_t ntiles = (nel + a.te - 1) / a.te;
+  const int grid = static_cast<int>(std::min<int64_t>(ntiles, static_cast<int64_t>(num_sms) * per_sm));
+  kern<<<grid, kMixedThreads, L.total, s>>>(a);
+  FEGPU_CUDA(cudaGetLastError());
+  return 1;
+}
+
+}  // namespace fegpu
