@@ -27,7 +27,7 @@ EXPORTS = [
     "fegpu_bilform_dot", "fegpu_linform_dot", "fegpu_matrix_nnz", "fegpu_matrix_copy_csc",
     "fegpu_matrix_copy_values", "fegpu_matrix_spmv", "fegpu_assembler_create",
     "fegpu_assembler_destroy", "fegpu_assembler_assemble", "fegpu_assembler_make",
-    "fegpu_assembler_copy_csc",
+    "fegpu_assembler_copy_csc", "fegpu_bilform_lin_elastic_noalloc",
 ]
 
 
@@ -84,6 +84,7 @@ def load(path: str = LIBPATH):
         "fegpu_assembler_assemble": ([vp, vp, i32, i32, vp, vp], i32),
         "fegpu_assembler_make": ([vp, p64], i32),
         "fegpu_assembler_copy_csc": ([vp, vp, vp, vp], i32),
+        "fegpu_bilform_lin_elastic_noalloc": ([vp, C.POINTER(Coef)], i32),
     }
     for name, (args, res) in proto.items():
         f = getattr(L, name)

@@ -83,6 +83,11 @@ int choose_tile(int etype, int form, int precision, int npts) {
   return te;
 }
 
+int mixed_tile_for(int etype, int npts) { return mixed_tile(etype, npts); }
+size_t mixed_smem_for(int etype, int npts, int te) {
+  return mixed_layout(nodes_per_elem(etype), manif_dim(etype), npts, te).total;
+}
+
 size_t form_smem_bytes(int etype, int form, int precision, int npts, int te) {
   const bool grad = form <= F_ELAST_GEN;
   const int tsize = (precision == FEGPU_MIXED && grad) ? 4 : 8;
@@ -172,6 +177,8 @@ void stage_coef(fegpu_femm *fm, const fegpu_coef *cf, int expect_ncomp, KArgs &a
   a.coef = st.sorted.as<double>();
 }
 
+}  // namespace
+
 KArgs base_args(fegpu_matrix *K, fegpu_dofmap *dm) {
   fegpu_femm *fm = dm->femm;
   KArgs a;
@@ -193,6 +200,8 @@ KArgs base_args(fegpu_matrix *K, fegpu_dofmap *dm) {
   a.distort_tol = 0.1;
   return a;
 }
+
+namespace {
 
 void run_colours(fegpu_dofmap *dm, int form, int precision, KArgs &a) {
   fegpu_femm *fm = dm->femm;
@@ -274,6 +283,8 @@ void require_geometry(fegpu_femm *fm) {
   FEGPU_REQUIRE(fm->has_geometry, "geometry not set (fegpu_femm_set_geometry)");
 }
 
+}  // namespace
+
 bool is_isotropic(const double *D, double &lam, double &mu) {
   const double a = D[0], b = D[1], c = D[3 * 6 + 3];
   for (int i = 0; i < 6; ++i)
@@ -289,6 +300,8 @@ bool is_isotropic(const double *D, double &lam, double &mu) {
   mu = c;
   return true;
 }
+
+namespace {
 
 }  // namespace
 }  // namespace fegpu

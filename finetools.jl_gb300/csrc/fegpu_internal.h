@@ -135,6 +135,13 @@ struct fegpu_dofmap {
   fegpu::DevBuf gnodes;     // int32: nodes in gather order
   fegpu::DevBuf pos_orig;   // uint16 [nelem][nne][nne], element order
   fegpu::DevBuf ke;         // float ring of element blocks
+  std::vector<int32_t> node_first, node_last;  // first / last incident element (-1: none)
+  // plan of the allocation-free variant (noalloc.cu), cached per chunk size
+  int64_t na_chunk = 0;
+  int na_ring = 0;
+  size_t na_coef_bytes = 0;
+  std::vector<int32_t> na_order;
+  std::vector<int64_t> na_chunk_nodes;
 };
 
 struct fegpu_matrix {
@@ -215,6 +222,16 @@ struct GArgs {
 };
 void build_gather_plan(fegpu_dofmap *dm, int nblk_values);
 int launch_gather(int etype, int ndn, const GArgs &g, int num_sms, cudaStream_t s);
+// variant that computes each element's ring slot from chunk and ring
+// (g.n2e_slot unused)
+int launch_gather_inline_slot(int etype, int ndn, const GArgs &g, int num_sms, cudaStream_t s);
+int launch_mixed(int etype, int form, const KArgs &a, int sms, cudaStream_t s);
+int mixed_tile_for(int etype, int npts);
+size_t mixed_smem_for(int etype, int npts, int te);
+
+// ---- shared by the entry points -----------------------------------------------------
+KArgs base_args(fegpu_matrix *K, fegpu_dofmap *dm);
+bool is_isotropic(const double *D, double &lam, double &mu);
 
 // ---- matrix utilities -----------------------------------------------------------
 void spmv(const fegpu_dofmap *dm, const double *val, const double *x, double *y,

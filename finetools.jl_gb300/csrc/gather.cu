@@ -90,7 +90,7 @@ __device__ __forceinline__ double ff_to_double(float h, float l) {
   return __longlong_as_double(static_cast<long long>(bits));
 }
 
-template <int NNE, int NDN>
+template <int NNE, int NDN, bool INLINE_SLOT>
 __global__ void __launch_bounds__(kWarpsPerCta * 32) k_gather(const GArgs g) {
   constexpr int NBLK = NNE * (NNE + 1) / 2;
   constexpr int BS = NDN * NDN;
@@ -116,7 +116,15 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) k_gather(const GArgs g) {
     for (int64_t q = g.n2e_ptr[A]; q < g.n2e_ptr[A + 1]; ++q) {
       const int64_t e = g.n2e_elem[q];
       const int a = g.n2e_loc[q];
-      const float *kb = g.ke + static_cast<int64_t>(g.n2e_slot[q]) * NBLK * BS;
+      int64_t slot;
+      if constexpr (INLINE_SLOT) {
+        const int32_t e32 = static_cast<int32_t>(e), ch = static_cast<int32_t>(g.chunk);
+        const int32_t ce = e32 / ch;
+        slot = static_cast<int64_t>(ce % g.ring) * ch + (e32 - ce * ch);
+      } else {
+        slot = g.n2e_slot[q];
+      }
+      const float *kb = g.ke + slot * NBLK * BS;
       const uint16_t *pe = g.pos + (e * NNE + a) * NNE;
       for (int task = lane; task < NNE * NDN; task += 32) {
         const int b = task / NDN, j = task - (task / NDN) * NDN;
@@ -145,13 +153,13 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) k_gather(const GArgs g) {
   }
 }
 
-template <int NNE, int NDN>
+template <int NNE, int NDN, bool INLINE_SLOT = false>
 int launch_t(const GArgs &g, int num_sms, cudaStream_t s) {
   const int64_t n = g.n1 - g.n0;
   if (n <= 0) return 0;
   const size_t smem = sizeof(float) * static_cast<size_t>(gather_warp_stride(NDN, g.maxdeg)) * kWarpsPerCta;
   FEGPU_REQUIRE(smem <= 227 * 1024, "node degree too large for the row gather");
-  auto kern = k_gather<NNE, NDN>;
+  auto kern = k_gather<NNE, NDN, INLINE_SLOT>;
   FEGPU_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   static_cast<int>(smem)));
   int per_sm = 0;
@@ -187,6 +195,17 @@ int launch_gather(int etype, int ndn, const GArgs &g, int num_sms, cudaStream_t 
   throw Error{FEGPU_ERR_ARG, "unknown element type"};
 }
 
+int launch_gather_inline_slot(int etype, int ndn, const GArgs &g, int num_sms, cudaStream_t s) {
+  switch (etype) {
+    case FEGPU_H8: return ndn == 1 ? launch_t<8, 1, true>(g, num_sms, s) : launch_t<8, 3, true>(g, num_sms, s);
+    case FEGPU_H20: return ndn == 1 ? launch_t<20, 1, true>(g, num_sms, s) : launch_t<20, 3, true>(g, num_sms, s);
+    case FEGPU_T4: return ndn == 1 ? launch_t<4, 1, true>(g, num_sms, s) : launch_t<4, 3, true>(g, num_sms, s);
+    case FEGPU_T10: return ndn == 1 ? launch_t<10, 1, true>(g, num_sms, s) : launch_t<10, 3, true>(g, num_sms, s);
+    case FEGPU_Q4: return ndn == 1 ? launch_t<4, 1, true>(g, num_sms, s) : launch_t<4, 3, true>(g, num_sms, s);
+  }
+  throw Error{FEGPU_ERR_ARG, "unknown element type"};
+}
+
 // Node -> element lists, chunk plan and element-order slot maps.
 void build_gather_plan(fegpu_dofmap *dm, int block_values) {
   fegpu_femm *fm = dm->femm;
@@ -215,6 +234,13 @@ void build_gather_plan(fegpu_dofmap *dm, int block_values) {
     }
   std::vector<int32_t> slot(elem.size());
   // a node is gathered after the chunk of its last element
+  dm->node_first.assign(N, -1);
+  dm->node_last.assign(N, -1);
+  for (int64_t n = 0; n < N; ++n)
+    if (ptr[n + 1] > ptr[n]) {
+      dm->node_first[n] = elem[ptr[n]];
+      dm->node_last[n] = elem[ptr[n + 1] - 1];
+    }
   std::vector<int64_t> cnt(nch + 1, 0);
   int64_t span = 0;
   for (int64_t n = 0; n < N; ++n) {

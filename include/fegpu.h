@@ -161,6 +161,24 @@ int fegpu_matrix_copy_values(fegpu_matrix *K, double *nzval);
 /* y = K x on the device (host vectors of length nalldofs) */
 int fegpu_matrix_spmv(fegpu_matrix *K, const double *x, double *y);
 
+/* Allocation-free mixed-precision bilform_lin_elastic.  No counterpart in the
+ * reference: it serves callers that cannot allocate device memory once they
+ * run -- a framework whose pool allocator has reserved the GPU, or a
+ * time-step loop that must not hit cudaMalloc's device-wide synchronisation.
+ * Same arguments and result as fegpu_bilform_lin_elastic(K, cf, FEGPU_MIXED);
+ * all scratch (element-block ring, node gather order, per-element
+ * coefficients) lives in one static device array of
+ * FEGPU_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until
+ * the process exits; meshes whose scratch would not fit are rejected with an
+ * error.  Calls no cudaMalloc or cudaFree.  Preconditions: one regular
+ * FEGPU_MIXED assembly on the same matrix has run (it builds the node-to-element
+ * tables read here).  The first call on a device looks up the array's device
+ * address; make that first call before any stream capture.  Calls share the
+ * array (it keeps the last call's contents): calls whose GPU work overlaps
+ * race. */
+#define FEGPU_NOALLOC_SCRATCH_BYTES (64u * 1024u * 1024u)
+int fegpu_bilform_lin_elastic_noalloc(fegpu_matrix *K, const fegpu_coef *cf);
+
 /* ---- generic assembler for element matrices formed on the host -----------
  * startassembly! / assemble! / makematrix! of SysmatAssemblerSparse(Symm)
  * (src/AssemblyModule.jl:209-329, 454-583) for FEMMs whose element matrices
