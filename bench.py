@@ -305,8 +305,8 @@ def run_ours(args):
     ft = entry.load_package()
     lib = Lib(ft, local)
     stream = torch.cuda.ExternalStream(lib.stream, device=local)
-    if args.only in ("h20", "h8"):
-        fn = bench_h20 if args.only == "h20" else bench_h8
+    if args.only in ("h20", "h8", "batch"):
+        fn = {"h20": bench_h20, "h8": bench_h8, "batch": bench_batch}[args.only]
         res = fn(ft, torch, lib, stream, args, local, dist)
         if rank == 0:
             print(json.dumps({"only": args.only, "workload": res}), flush=True)
@@ -386,6 +386,8 @@ def run_ours(args):
     if not args.headline_only and args.only is None:
         workloads["h20_40_elasticity"] = bench_h20(ft, torch, lib, stream, args, local, dist)
         workloads["h8_20_diffusion"] = bench_h8(ft, torch, lib, stream, args, local, dist)
+        workloads["batch_256_mixed_types"] = bench_batch(ft, torch, lib, stream, args, local,
+                                                         dist)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -476,6 +478,132 @@ def bench_h20(ft, torch, lib, stream, args, local, dist):
     return res
 
 
+BATCH_TYPES = ("H8", "H20", "T4", "T10", "Q4")
+
+
+def batch_cases(ft, count, seed=5, emin=1e3, emax=2e5, device=0):
+    """The mixed-type batch: `count` meshes with log-uniform element counts on
+    [emin, emax], types uniform over H8/H20/T4/T10/Q4 (Q4: surface mass by the
+    dot form, thickness 0.01), each non-Q4 mesh diffusion or elasticity at
+    random, seeded per-element coefficients."""
+    rng = np.random.default_rng(seed)
+    rules = {"H8": lambda: ft.GaussRule(3, 2), "H20": lambda: ft.GaussRule(3, 3),
+             "T4": lambda: ft.TetRule(1), "T10": lambda: ft.TetRule(4),
+             "Q4": lambda: ft.GaussRule(2, 2)}
+    cases = []
+    for _ in range(count):
+        n = int(round(np.exp(rng.uniform(np.log(emin), np.log(emax)))))
+        et = BATCH_TYPES[int(rng.integers(len(BATCH_TYPES)))]
+        fens, fes = ft.nearest_block(et, n, seed=int(rng.integers(1 << 31)))
+        E = fes.count()
+        if et == "Q4":
+            form, ndn = "dot", 3
+            femm = ft.FEMMBase(ft.IntegDomain(fes, rules[et](), 0.01), device=device)
+            cf = ft.ElementwiseData(rng.lognormal(np.log(7.8e3), 0.3, E))
+        else:
+            femm = ft.FEMMBase(ft.IntegDomain(fes, rules[et]()), device=device)
+            if rng.random() < 0.5:
+                form, ndn = "diffusion", 1
+                cf = ft.ElementwiseData(rng.lognormal(0.0, 0.5, E))
+            else:
+                form, ndn = "lin_elastic", 3
+                cf = ft.IsotropicElementwise(rng.lognormal(np.log(70e9), 0.5, E),
+                                             rng.uniform(0.2, 0.35, E))
+        geom = ft.NodalField(fens.xyz)
+        u = ft.numberdofs(ft.NodalField(np.zeros((fens.count(), ndn))))
+        cases.append({"type": et, "form": form, "femm": femm, "geom": geom, "u": u, "cf": cf,
+                      "elements": E, "nodes": fens.count()})
+    return cases
+
+
+def _single_call(ft, c, asm):
+    if c["form"] == "diffusion":
+        return ft.bilform_diffusion(c["femm"], asm, c["geom"], c["u"], c["cf"])
+    if c["form"] == "lin_elastic":
+        return ft.bilform_lin_elastic(c["femm"], asm, c["geom"], c["u"], ft.DeforModelRed3D,
+                                      c["cf"])
+    return ft.bilform_dot(c["femm"], asm, c["geom"], c["u"], c["cf"], m=3)
+
+
+def bench_batch(ft, torch, lib, stream, args, local, dist):
+    t0 = time.perf_counter()
+    cases = batch_cases(ft, args.batch_meshes, device=local)
+    mesh_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    b = ft.AssemblyBatch(device=local)
+    mats = [b.add(c["form"], c["femm"], c["geom"], c["u"], c["cf"], m=3) for c in cases]
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    b.tune()
+    tune_s = time.perf_counter() - t0
+    st = b.stats()
+
+    def step():
+        lib.nat.check(lib.L.fegpu_batch_launch(b.h))
+
+    lib.stats(reset=True)
+    ms = time_steps(torch, stream, step, args.steps, args.warmup, dist=dist)
+    b.wait()
+    _, launches = lib.stats(reset=True)
+    ms_step = ms / args.steps
+    E = sum(c["elements"] for c in cases)
+    nnz = sum(M.dm.nnz for M in mats)
+    B = 0
+    for c, M in zip(cases, mats):
+        nne = c["femm"].integdomain.fes.conn.shape[1]
+        s_coef = 16 if c["form"] == "lin_elastic" else 8
+        B += algorithmic_bytes(c["elements"], nne, c["nodes"], M.dm.nnz, M.dm.ndof, s_coef)
+    peak, _ = measured_peaks()
+    res = {"meshes": len(cases), "elements": E, "nnz": nnz, "work_items": st["items"],
+           "types": {t: sum(1 for c in cases if c["type"] == t) for t in BATCH_TYPES},
+           "forms": {f: sum(1 for c in cases if c["form"] == f)
+                     for f in ("diffusion", "lin_elastic", "dot")},
+           "ms_per_step": ms_step, "elements_per_s": E / (ms_step * 1e-3),
+           "nnz_per_s": nnz / (ms_step * 1e-3), "algorithmic_bytes": B,
+           "hbm_frac": B / (ms_step * 1e-3) / 1e9 / peak,
+           "gpu_launches_per_step": launches / (args.steps + args.warmup),
+           "setup_s": {"meshes": mesh_s, "patterns_and_jobs": setup_s, "autotune": tune_s},
+           "tiles": {t: sorted({b.tile(j) for j, c in enumerate(cases) if c["type"] == t})
+                     for t in BATCH_TYPES}}
+    # the same jobs one call at a time (mixed, then FP64), and the accuracy
+    seq = {}
+    refs = {}
+    for prec in ("mixed", "fp64"):
+        asm = ft.SysmatAssemblerGPU(precision=prec, result="device", device=local)
+        Ks = [_single_call(ft, c, asm) for c in cases]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for c in cases:
+            _single_call(ft, c, asm)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        seq[prec] = {"elements_per_s": E / dt, "ms": 1e3 * dt}
+        refs[prec] = Ks
+    res["one_call_per_mesh"] = seq
+    res["speedup_over_one_call_per_mesh_mixed"] = seq["mixed"]["ms"] / ms_step
+    rng = np.random.default_rng(3)
+    worst_kx, worst_entry, identical = 0.0, 0.0, True
+    small = [j for j, M in enumerate(mats) if M.dm.nnz <= 30_000_000]  # host copies stay small
+    sample = set(rng.choice(small, size=min(8, len(small)), replace=False).tolist()) if small \
+        else set()
+    for j, (M, K64, K32) in enumerate(zip(mats, refs["fp64"], refs["mixed"])):
+        x = rng.uniform(-1, 1, M.shape[0])
+        y, y64 = M.spmv(x), K64.spmv(x)
+        worst_kx = max(worst_kx, float(np.linalg.norm(y - y64) / np.linalg.norm(y64)))
+        if j in sample:
+            v, v64 = M.values(), K64.values()
+            worst_entry = max(worst_entry, float(np.abs(v - v64).max() / np.abs(v64).max()))
+            if cases[j]["form"] != "dot":
+                identical &= bool(np.array_equal(v, K32.values()))
+    res["vs_fp64"] = {"max_rel_Kx": worst_kx, "max_abs_over_max_sampled": worst_entry,
+                      "sampled_meshes": len(sample)}
+    res["identical_to_one_call_mixed_sampled"] = identical
+    del refs, mats, b
+    torch.cuda.empty_cache()
+    return res
+
+
 def bench_h8(ft, torch, lib, stream, args, local, dist):
     fens, fes = ft.h8_diffusion_mesh(n=H8_N)
     geom = ft.NodalField(fens.xyz)
@@ -509,9 +637,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--headline-only", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--only", choices=["t10", "h20", "h8"], default=None,
+    ap.add_argument("--only", choices=["t10", "h20", "h8", "batch"], default=None,
                     help="run one workload only (profiling); prints its numbers")
     ap.add_argument("--h20-n", type=int, default=H20_N)
+    ap.add_argument("--batch-meshes", type=int, default=256,
+                    help="meshes of the mixed-type batch workload")
     ap.add_argument("--t10-n", type=int, default=T10_N,
                     help="cells per side of the headline T10 block (60 = the benchmark size)")
     args = ap.parse_args()

@@ -9,6 +9,7 @@ sm_103a CUDA kernels behind the C ABI of include/fegpu.h (libfegpu.so); this
 package is the host-side mirror of the reference's Julia interface.
 """
 from ._native import FegpuError, load as load_library
+from .batch import AssemblyBatch
 from .assembly import (DeviceMatrix, SysmatAssemblerGPU, SysvecAssemblerGPU, assemble,
                        makematrix, startassembly)
 from .femm import (DataCache, DeforModelRed3D, ElementwiseData, FEMMBase, ForceIntensity,
@@ -19,7 +20,8 @@ from .fesets import FESetH8, FESetH20, FESetQ4, FESetT4, FESetT10
 from .fields import DOF_KIND_DATA, DOF_KIND_FREE, NodalField, gathersysvec, numberdofs, setebc
 from .meshes import (FENodeSet, H8block, H8blockx, H8toH20, H20block, Q4block, Q4blockx,
                      T4block, T4blockx, T4toT10, T10block, h8_diffusion_mesh,
-                     h20_elastic_mesh, isotropic_D, lame, linearspace, t10_elastic_mesh)
+                     h20_elastic_mesh, isotropic_D, lame, linearspace, nearest_block,
+                     t10_elastic_mesh)
 from .rules import GaussRule, TetRule
 
 __all__ = [n for n in dir() if not n.startswith("_")]

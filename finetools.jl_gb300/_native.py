@@ -16,6 +16,7 @@ OK = 0
 Q4, H8, H20, T4, T10 = 0, 1, 2, 3, 4
 COEF_CONST, COEF_PER_ELEMENT, COEF_PER_QP, COEF_ISO_LAME = 0, 1, 2, 3
 FP64, MIXED = 0, 1
+FORM_DIFFUSION, FORM_LIN_ELASTIC, FORM_DOT = 0, 1, 2
 
 EXPORTS = [
     "fegpu_last_error", "fegpu_context_create", "fegpu_context_destroy",
@@ -28,6 +29,9 @@ EXPORTS = [
     "fegpu_matrix_copy_values", "fegpu_matrix_spmv", "fegpu_assembler_create",
     "fegpu_assembler_destroy", "fegpu_assembler_assemble", "fegpu_assembler_make",
     "fegpu_assembler_copy_csc", "fegpu_bilform_lin_elastic_noalloc",
+    "fegpu_batch_create", "fegpu_batch_destroy", "fegpu_batch_add", "fegpu_batch_set_coef",
+    "fegpu_batch_tune", "fegpu_batch_tile", "fegpu_batch_set_wait_limit", "fegpu_batch_launch",
+    "fegpu_batch_wait", "fegpu_batch_run", "fegpu_batch_stats",
 ]
 
 
@@ -85,6 +89,17 @@ def load(path: str = LIBPATH):
         "fegpu_assembler_make": ([vp, p64], i32),
         "fegpu_assembler_copy_csc": ([vp, vp, vp, vp], i32),
         "fegpu_bilform_lin_elastic_noalloc": ([vp, C.POINTER(Coef)], i32),
+        "fegpu_batch_create": ([vp, pp], i32),
+        "fegpu_batch_destroy": ([vp], i32),
+        "fegpu_batch_add": ([vp, vp, i32, C.POINTER(Coef), i32, p64], i32),
+        "fegpu_batch_set_coef": ([vp, i64, C.POINTER(Coef)], i32),
+        "fegpu_batch_tune": ([vp, C.c_char_p], i32),
+        "fegpu_batch_tile": ([vp, i64, C.POINTER(C.c_int)], i32),
+        "fegpu_batch_set_wait_limit": ([vp, d], i32),
+        "fegpu_batch_launch": ([vp], i32),
+        "fegpu_batch_wait": ([vp], i32),
+        "fegpu_batch_run": ([vp], i32),
+        "fegpu_batch_stats": ([vp, p64, p64], i32),
     }
     for name, (args, res) in proto.items():
         f = getattr(L, name)

@@ -83,7 +83,7 @@ int choose_tile(int etype, int form, int precision, int npts) {
   return te;
 }
 
-int mixed_tile_for(int etype, int npts) { return mixed_tile(etype, npts); }
+int mixed_tile_for(int etype, int npts) { return default_mixed_tile(etype, npts); }
 size_t mixed_smem_for(int etype, int npts, int te) {
   return mixed_layout(nodes_per_elem(etype), manif_dim(etype), npts, te).total;
 }
@@ -234,7 +234,7 @@ void run_gather(fegpu_dofmap *dm, int form, KArgs &a) {
   const int bs = ndn * ndn, nblk = nne * (nne + 1) / 2;
   if (!dm->gather_ready) build_gather_plan(dm, nblk * bs);
   a.conn = fm->conn_orig.as<int32_t>();
-  a.te = mixed_tile(fm->etype, fm->npts);
+  a.te = default_mixed_tile(fm->etype, fm->npts);
   FEGPU_REQUIRE(mixed_layout(nne, fm->mdim, fm->npts, a.te).total <= 227 * 1024,
                 "quadrature rule too large for the element kernel");
   GArgs g;
@@ -444,8 +444,8 @@ int fegpu_femm_create(fegpu_context *ctx, int etype, int64_t nelem, const int64_
     fm->tab.alloc(sizeof(double) * tab.size());
     FEGPU_CUDA(cudaMemcpyAsync(fm->tab.p, tab.data(), sizeof(double) * tab.size(),
                                cudaMemcpyHostToDevice, s));
-    std::vector<float> tab32(static_cast<size_t>(npts) * nne * mdim + npts);
-    for (size_t i = 0; i < tab32.size(); ++i) tab32[i] = static_cast<float>(tab[npts * nne + i]);
+    std::vector<float> tab32(tab.size());  // N, dN, w in FP32
+    for (size_t i = 0; i < tab32.size(); ++i) tab32[i] = static_cast<float>(tab[i]);
     fm->tab32.alloc(sizeof(float) * tab32.size());
     FEGPU_CUDA(cudaMemcpyAsync(fm->tab32.p, tab32.data(), sizeof(float) * tab32.size(),
                                cudaMemcpyHostToDevice, s));

@@ -104,7 +104,7 @@ struct fegpu_femm {
   fegpu::DevBuf conn;                  // int32 nelem x nne, colour-sorted
   fegpu::DevBuf perm;                  // int32 sorted position -> element
   fegpu::DevBuf tab;                   // double: N[q][k], dN[q][k][m], w[q]
-  fegpu::DevBuf tab32;                 // float: dN[q][k][m], w[q]
+  fegpu::DevBuf tab32;                 // float: N[q][k], dN[q][k][m], w[q]
   fegpu::DevBuf xyz;                   // double [nnodes][4]
   bool has_geometry = false;
   std::vector<int32_t> conn_host;      // element order, 0-based
@@ -166,7 +166,7 @@ struct KArgs {
   const int32_t *conn;     // colour-sorted nelem x nne
   const double *xyz;       // [nnodes][4]
   const double *tab;       // N, dN, w tables
-  const float *tab32;      // FP32 dN and w tables (mixed path)
+  const float *tab32;      // FP32 N, dN and w tables (mixed path)
   const uint16_t *pos;     // colour-sorted nelem x nne x nne
   const int32_t *dof;      // [nnodes][ndn]
   const int64_t *rowptr;   // CSR rows

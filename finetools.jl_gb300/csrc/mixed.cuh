@@ -114,18 +114,22 @@ __device__ void jacobian_fp64(const double *xyz, const int32_t *conn, const doub
   }
 }
 
+// One tile: elements [eb, eb + ne) of the launch range starting at a.e0.
+// Blocks of element e go to ke + (e - e0) * nblk * ndn^2.
 template <int ET, int FORM, int NDN>
-__global__ void __launch_bounds__(kMixedThreads) k_blocks_mixed(const KArgs a) {
+__device__ __forceinline__ void mixed_tile(const KArgs &a, int64_t eb, int ne,
+                                           unsigned char *smem, float *ke, int64_t e0) {
   constexpr int NNE = ElemT<ET>::NNE, MDIM = ElemT<ET>::MDIM;
   constexpr int NBLK = NNE * (NNE + 1) / 2;
   constexpr int NGRP = mixed_groups(NNE);
   constexpr int BS = NDN * NDN;
-  extern __shared__ __align__(16) unsigned char smem[];
+  constexpr bool GRAD = FORM != F_DOT;
   const int npts = a.npts, te = a.te;
   const MixedLayout L = mixed_layout(NNE, MDIM, npts, te);
-  // FP32 tables live in global memory (read through L1): dN[q][k][m], then w[q]
-  const float *fdN = a.tab32;
-  const float *fw = a.tab32 + npts * NNE * MDIM;
+  // FP32 tables live in global memory (read through L1): N[q][k], dN[q][k][m], w[q]
+  const float *fN = a.tab32;
+  const float *fdN = a.tab32 + npts * NNE;
+  const float *fw = fdN + npts * NNE * MDIM;
   float *sJ = reinterpret_cast<float *>(smem + L.jac);
   float *sLame = reinterpret_cast<float *>(smem + L.lame);
   int32_t *sConn = reinterpret_cast<int32_t *>(smem + L.conn);
@@ -139,12 +143,7 @@ __global__ void __launch_bounds__(kMixedThreads) k_blocks_mixed(const KArgs a) {
   const double *tabdN = a.tab + npts * NNE;
   const float tol = static_cast<float>(a.distort_tol);
   const float odim = static_cast<float>(a.otherdim);
-  const int64_t nel = a.e1 - a.e0;
-  const int64_t ntiles = (nel + te - 1) / te;
-
-  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const int64_t eb = a.e0 + tile * te;
-    const int ne = static_cast<int>(min(static_cast<int64_t>(te), a.e1 - eb));
+  {
     __syncthreads();
     for (int i = tid; i < ne * NNE; i += nth) sConn[i] = a.conn[eb * NNE + i];
     __syncthreads();
@@ -194,7 +193,20 @@ __global__ void __launch_bounds__(kMixedThreads) k_blocks_mixed(const KArgs a) {
         for (int m = 0; m < MDIM; ++m) J[s][m] = sJ[i * 9 + s * 3 + m];
       float *inv = sJinv + i * 9;
       float det;
-      if constexpr (MDIM == 3) {
+      if constexpr (!GRAD) {
+        if constexpr (MDIM == 3) {
+          det = J[0][0] * (J[1][1] * J[2][2] - J[2][1] * J[1][2]) -
+                J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+        } else if (a.sdim == 2) {
+          det = J[0][0] * J[1][1] - J[1][0] * J[0][1];
+        } else {
+          const float c1 = J[1][0] * J[2][1] - J[2][0] * J[1][1];
+          const float c2 = J[2][0] * J[0][1] - J[0][0] * J[2][1];
+          const float c3 = J[0][0] * J[1][1] - J[1][0] * J[0][1];
+          det = sqrtf(c1 * c1 + c2 * c2 + c3 * c3);
+        }
+      } else if constexpr (MDIM == 3) {
         const float c0 = J[1][1] * J[2][2] - J[2][1] * J[1][2];
         const float c1 = J[1][0] * J[2][2] - J[1][2] * J[2][0];
         const float c2 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
@@ -230,7 +242,7 @@ __global__ void __launch_bounds__(kMixedThreads) k_blocks_mixed(const KArgs a) {
         dmax = fmaxf(dmax, v);
       }
       float det = sDet[i];
-      if (!(dmin > tol * dmax)) {
+      if (GRAD && !(dmin > tol * dmax)) {
         double inv[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, dd;
         jacobian_fp64<NNE, MDIM>(a.xyz, sConn + e * NNE, tabdN + q * NNE * MDIM, a.sdim, inv, dd);
 #pragma unroll
@@ -238,8 +250,8 @@ __global__ void __launch_bounds__(kMixedThreads) k_blocks_mixed(const KArgs a) {
         det = float(dd);
       }
       float w = det * fw[q];
-      if (MDIM == 2) w *= odim;
-      if constexpr (FORM == F_DIFF_ISO) {
+      if (MDIM == 2 && (GRAD || a.measure_m == 3)) w *= odim;
+      if constexpr (FORM == F_DIFF_ISO || FORM == F_DOT) {
         float c = 1.f;
         if (a.coef_kind == FEGPU_COEF_CONST) c = float(a.cconst[0]);
         else if (a.coef_kind == FEGPU_COEF_PER_ELEMENT) c = float(a.coef[eb + e]);
@@ -250,7 +262,7 @@ __global__ void __launch_bounds__(kMixedThreads) k_blocks_mixed(const KArgs a) {
     }
     __syncthreads();
     // C. gradients and weighted gradients per (element, point, node)
-    for (int i = tid; i < ne * npts * NNE; i += nth) {
+    for (int i = tid; i < (GRAD ? ne * npts * NNE : 0); i += nth) {
       const int eq = i / NNE, k = i - eq * NNE;
       const int q = eq - (eq / npts) * npts;
       const float *inv = sJinv + eq * 9;
@@ -299,7 +311,16 @@ __global__ void __launch_bounds__(kMixedThreads) k_blocks_mixed(const KArgs a) {
           for (int n = 0; n < 3; ++n) M[u][m][n] = 0.f;
       const float4 *wa = sWG + (e * npts) * NNE + pa;
       const float4 *gb = sG + (e * npts) * NNE + b0;
-      for (int q = 0; q < npts; ++q) {
+      if constexpr (!GRAD) {
+        // dot: s_ab = sum_q N_a N_b (Jac w c)_q  (src/FEMMBaseModule.jl:1357-1361)
+        for (int q = 0; q < npts; ++q) {
+          const float wna = sJw[e * npts + q] * fN[q * NNE + pa];
+#pragma unroll
+          for (int u = 0; u < 4; ++u)
+            if (u < nb) M[u][0][0] = fmaf(wna, fN[q * NNE + b0 + u], M[u][0][0]);
+        }
+      }
+      for (int q = 0; q < (GRAD ? npts : 0); ++q) {
         const float4 x = wa[q * NNE];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
@@ -325,7 +346,7 @@ __global__ void __launch_bounds__(kMixedThreads) k_blocks_mixed(const KArgs a) {
       }
       const double *D = (FORM == F_ELAST_GEN && a.coef_kind == FEGPU_COEF_PER_ELEMENT)
                              ? a.coef + es * 36 : a.cconst;
-      float *kb = a.ke + static_cast<int64_t>(eb + e - a.e0) * NBLK * BS;
+      float *kb = ke + static_cast<int64_t>(eb + e - e0) * NBLK * BS;
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
         if (u >= nb) break;
@@ -333,6 +354,13 @@ __global__ void __launch_bounds__(kMixedThreads) k_blocks_mixed(const KArgs a) {
         float *out = kb + (pa * NNE - pa * (pa - 1) / 2 + (pb - pa)) * BS;
         if constexpr (FORM == F_DIFF_ISO || FORM == F_DIFF_GEN) {
           out[0] = M[u][0][0];
+        } else if constexpr (FORM == F_DOT) {
+          // block = s * c (c: the symmetric-assembler arrangement set by the host)
+          const double *cm = (pb == pa) ? a.cdiag : a.cab;
+#pragma unroll
+          for (int ii = 0; ii < NDN; ++ii)
+#pragma unroll
+            for (int jj = 0; jj < NDN; ++jj) out[ii * NDN + jj] = M[u][0][0] * float(cm[ii * NDN + jj]);
         } else {
           float V[3][3];
           if constexpr (FORM == F_ELAST_ISO) {
@@ -372,9 +400,21 @@ __global__ void __launch_bounds__(kMixedThreads) k_blocks_mixed(const KArgs a) {
   }
 }
 
+template <int ET, int FORM, int NDN>
+__global__ void __launch_bounds__(kMixedThreads) k_blocks_mixed(const KArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int64_t nel = a.e1 - a.e0;
+  const int64_t ntiles = (nel + a.te - 1) / a.te;
+  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int64_t eb = a.e0 + tile * a.te;
+    const int ne = static_cast<int>(min(static_cast<int64_t>(a.te), a.e1 - eb));
+    mixed_tile<ET, FORM, NDN>(a, eb, ne, smem, a.ke, a.e0);
+  }
+}
+
 // Elements per tile: enough Gram tasks for two passes of the CTA, within a
 // shared-memory budget that leaves two CTAs per SM.
-inline int mixed_tile(int etype, int npts) {
+inline int default_mixed_tile(int etype, int npts) {
   const int nne = nodes_per_elem(etype), mdim = manif_dim(etype);
   const size_t budget = 72 * 1024;
   const MixedLayout one = mixed_layout(nne, mdim, npts, 1);

@@ -240,6 +240,32 @@ def _neighbours_valid(xyz, conn, node, newpos, dN):
     return True
 
 
+def nearest_block(etype: str, nelem: int, seed: int, amplitude: float = 0.15):
+    """Unit block of about nelem elements of type etype ("H8", "H20", "T4",
+    "T10" or "Q4"): the nx x ny (x nz) cell grid closest to the request (six
+    tetrahedra per cell), vertices strictly inside jittered by +-amplitude*h,
+    mid-edge nodes of quadratic elements recomputed as edge means."""
+    if etype == "Q4":
+        nx = max(1, int(round(np.sqrt(nelem))))
+        ny = max(1, int(round(nelem / nx)))
+        fens, fes = Q4block(1.0, 1.0, nx, ny)
+        fens.xyz = jitter_interior(fens.xyz, (nx, ny), amplitude, seed, box=(1.0, 1.0))
+        return fens, fes
+    tets = etype in ("T4", "T10")
+    cells = nelem / 6.0 if tets else float(nelem)
+    nx = max(1, int(round(cells ** (1.0 / 3.0))))
+    nz = max(1, int(round(cells / (nx * nx))))
+    fens, fes = (T4block if tets else H8block)(1.0, 1.0, 1.0, nx, nx, nz)
+    fens.xyz = jitter_interior(fens.xyz, (nx, nx, nz), amplitude, seed)
+    if etype in ("H20", "T10"):
+        nv = fens.xyz.shape[0]
+        fens, fes = (T4toT10 if tets else H8toH20)(fens, fes)
+        fens = recompute_midpoints(fens, fes, nv)
+    elif etype not in ("H8", "T4"):
+        raise ValueError(f"unknown element type {etype}")
+    return fens, fes
+
+
 def lame(E, nu):
     """Lame constants of an isotropic material."""
     E = np.asarray(E, dtype=np.float64)

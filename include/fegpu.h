@@ -179,6 +179,45 @@ int fegpu_matrix_spmv(fegpu_matrix *K, const double *x, double *y);
 #define FEGPU_NOALLOC_SCRATCH_BYTES (64u * 1024u * 1024u)
 int fegpu_bilform_lin_elastic_noalloc(fegpu_matrix *K, const fegpu_coef *cf);
 
+/* ---- batches: many assemblies in one persistent launch ---------------------
+ * A batch replaces a host loop of bilform calls over many FEMMs -- each one
+ * bilform_diffusion (src/FEMMBaseModule.jl:1462-1545), bilform_lin_elastic
+ * (1774-1824) or bilform_dot (1335-1376) with SysmatAssemblerSparseSymm --
+ * by one persistent kernel over a work queue of element tiles and row-gather
+ * ranges of all of them (any mix of element types and sizes), replayed as a
+ * CUDA graph.  Every job is evaluated as the FEGPU_MIXED path and its matrix
+ * is identical to fegpu_bilform_*(K, cf, FEGPU_MIXED) (bilform_dot: the
+ * symmetric arrangement).  Batched kinds: diffusion (scalar coefficient:
+ * constant, per element or per point) on Q4/H8/H20/T4/T10; linear elasticity
+ * (isotropic D or per-element Lame pairs) on H8/H20/T4/T10; dot (scalar
+ * coefficient, or a constant ndn x ndn matrix; ndn 1 or 3) on Q4 (m = 2 or
+ * 3) and H8.  Each matrix takes part in at most one job of a batch.
+ * Waits inside the kernel are bounded (default 5 s each,
+ * fegpu_batch_set_wait_limit): one that runs out makes fegpu_batch_wait /
+ * run return FEGPU_ERR_DEVICE. */
+#define FEGPU_FORM_DIFFUSION 0
+#define FEGPU_FORM_LIN_ELASTIC 1
+#define FEGPU_FORM_DOT 2
+typedef struct fegpu_batch fegpu_batch;
+int fegpu_batch_create(fegpu_context *ctx, fegpu_batch **out);
+int fegpu_batch_destroy(fegpu_batch *b);
+/* adds a job; its index goes to *job (may be null).  m: dot manifold
+ * dimension (ignored by the other forms).  Coefficient values are copied. */
+int fegpu_batch_add(fegpu_batch *b, fegpu_matrix *K, int form, const fegpu_coef *cf,
+                    int m, int64_t *job);
+/* new coefficient values for a job (same form); the captured graph stays */
+int fegpu_batch_set_coef(fegpu_batch *b, int64_t job, const fegpu_coef *cf);
+/* autotuner: elements per tile for each job kind, timed on the largest job
+ * of that kind; cache_path (or null) keeps "<kind> <tile>" lines across runs */
+int fegpu_batch_tune(fegpu_batch *b, const char *cache_path);
+int fegpu_batch_tile(fegpu_batch *b, int64_t job, int *elements_per_tile);
+int fegpu_batch_set_wait_limit(fegpu_batch *b, double seconds);
+/* launch (asynchronous, on the context stream) / wait and check / both */
+int fegpu_batch_launch(fegpu_batch *b);
+int fegpu_batch_wait(fegpu_batch *b);
+int fegpu_batch_run(fegpu_batch *b);
+int fegpu_batch_stats(fegpu_batch *b, int64_t *jobs, int64_t *items);
+
 /* ---- generic assembler for element matrices formed on the host -----------
  * startassembly! / assemble! / makematrix! of SysmatAssemblerSparse(Symm)
  * (src/AssemblyModule.jl:209-329, 454-583) for FEMMs whose element matrices
