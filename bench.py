@@ -348,7 +348,7 @@ def run_ours(args):
     B = algorithmic_bytes(E, 10, N, nnz, ndof, 0)
     peak, peak_src = measured_peaks()
     achieved = B / (kernel_ms_step * 1e-3) / 1e9
-    traffic = traffic_record().get("t10_fp64")
+    traffic = traffic_record().get("t10_fp64", {}).get("bytes_per_assembly")
     fp64_peak = fp64_peak_tflops(torch)
     flops = elastic_flops_per_element(10, 4) * E
 
