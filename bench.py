@@ -305,8 +305,9 @@ def run_ours(args):
     ft = entry.load_package()
     lib = Lib(ft, local)
     stream = torch.cuda.ExternalStream(lib.stream, device=local)
-    if args.only in ("h20", "h8", "batch"):
-        fn = {"h20": bench_h20, "h8": bench_h8, "batch": bench_batch}[args.only]
+    if args.only in ("h20", "h8", "batch", "serve"):
+        fn = {"h20": bench_h20, "h8": bench_h8, "batch": bench_batch,
+              "serve": bench_serve}[args.only]
         res = fn(ft, torch, lib, stream, args, local, dist)
         if rank == 0:
             print(json.dumps({"only": args.only, "workload": res}), flush=True)
@@ -388,6 +389,8 @@ def run_ours(args):
         workloads["h8_20_diffusion"] = bench_h8(ft, torch, lib, stream, args, local, dist)
         workloads["batch_256_mixed_types"] = bench_batch(ft, torch, lib, stream, args, local,
                                                          dist)
+        workloads["serve_32_resident_meshes"] = bench_serve(ft, torch, lib, stream, args, local,
+                                                            dist)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -465,8 +468,28 @@ def bench_h20(ft, torch, lib, stream, args, local, dist):
                      "kernel_ms": kstep, "hbm_frac": B / (kstep * 1e-3) / 1e9 / peak,
                      "algorithmic_bytes": B}
         mats[prec] = K
-    v64 = mats["fp64"].values()
+    # the same mixed assembly as a one-job persistent launch (element tiles of
+    # chunk c+1 overlap the gather of chunk c)
+    b = ft.AssemblyBatch(device=local)
+    Mb = b.add("lin_elastic", femm, geom, u, cf)
+
+    def bstep():
+        lib.nat.check(lib.L.fegpu_batch_launch(b.h))
+
+    lib.stats(reset=True)
+    ms = time_steps(torch, stream, bstep, args.steps, args.warmup, dist=dist)
+    b.wait()
+    lib.stats(reset=True)
+    ms_step = ms / args.steps
+    B = algorithmic_bytes(fes.count(), 20, fens.count(), Mb.dm.nnz, Mb.dm.ndof, 16)
+    res["mixed_persistent"] = {"elements_per_s": fes.count() / (ms_step * 1e-3),
+                               "ms_per_step": ms_step,
+                               "hbm_frac": B / (ms_step * 1e-3) / 1e9 / measured_peaks()[0],
+                               "work_items": b.stats()["items"]}
     v32 = mats["mixed"].values()
+    res["mixed_persistent"]["identical_to_mixed"] = bool(np.array_equal(Mb.values(), v32))
+    del b, Mb
+    v64 = mats["fp64"].values()
     x = np.random.default_rng(3).uniform(-1, 1, mats["fp64"].shape[0])
     y64 = mats["fp64"].spmv(x)
     y32 = mats["mixed"].spmv(x)
@@ -599,9 +622,191 @@ def bench_batch(ft, torch, lib, stream, args, local, dist):
     res["vs_fp64"] = {"max_rel_Kx": worst_kx, "max_abs_over_max_sampled": worst_entry,
                       "sampled_meshes": len(sample)}
     res["identical_to_one_call_mixed_sampled"] = identical
-    del refs, mats, b
+    del refs, mats, b, cases
+    import gc
+    gc.collect()
     torch.cuda.empty_cache()
     return res
+
+
+def serve_cases(ft, count, seed=6, emin=1e4, emax=2e6, device=0):
+    """Resident meshes of the serving workload: `count` H8 or T10 blocks with
+    log-uniform element counts on [emin, emax]; H8 meshes carry diffusion with a
+    per-element conductivity, T10 meshes elasticity with per-element (E, nu)."""
+    rng = np.random.default_rng(seed)
+    cases = []
+    for _ in range(count):
+        n = int(round(np.exp(rng.uniform(np.log(emin), np.log(emax)))))
+        et = "H8" if rng.random() < 0.5 else "T10"
+        fens, fes = ft.nearest_block(et, n, seed=int(rng.integers(1 << 31)))
+        E = fes.count()
+        if et == "H8":
+            form, ndn = "diffusion", 1
+            femm = ft.FEMMBase(ft.IntegDomain(fes, ft.GaussRule(3, 2)), device=device)
+            cf = ft.ElementwiseData(rng.lognormal(0.0, 1.0, E))
+        else:
+            form, ndn = "lin_elastic", 3
+            femm = ft.FEMMBase(ft.IntegDomain(fes, ft.TetRule(4)), device=device)
+            cf = ft.IsotropicElementwise(rng.lognormal(np.log(70e9), 1.0, E), np.full(E, 0.3))
+        cases.append({"type": et, "form": form, "femm": femm, "geom": ft.NodalField(fens.xyz),
+                      "u": ft.numberdofs(ft.NodalField(np.zeros((fens.count(), ndn)))),
+                      "cf": cf, "elements": E, "nodes": fens.count(), "xyz": fens.xyz,
+                      "h": 1.0 / round((E / (6.0 if et == "T10" else 1.0)) ** (1.0 / 3.0))})
+    return cases
+
+
+def _request_payloads(cases, rng):
+    """Two coefficient vectors (lognormal, sigma 1) and two coordinate sets
+    (interior nodes moved by +-0.05 h) per mesh, made once."""
+    out = []
+    for c in cases:
+        E = c["elements"]
+        if c["form"] == "diffusion":
+            coefs = [rng.lognormal(0.0, 1.0, E) for _ in range(2)]
+        else:
+            coefs = []
+            for _ in range(2):
+                lam, mu = ftlame(rng.lognormal(np.log(70e9), 1.0, E), 0.3)
+                coefs.append(np.ascontiguousarray(np.stack([lam, mu], axis=1)))
+        xyz = c["xyz"]
+        inside = np.all((xyz > 1e-9) & (xyz < 1 - 1e-9), axis=1)
+        coords = []
+        for _ in range(2):
+            x = xyz.copy()
+            x[inside] += rng.uniform(-0.05, 0.05, (int(inside.sum()), 3)) * c["h"]
+            coords.append(np.asfortranarray(x))
+        out.append({"coef": coefs, "coords": coords})
+    return out
+
+
+def ftlame(E, nu):
+    lam = E * nu / ((1 + nu) * (1 - 2 * nu))
+    mu = E / (2 * (1 + nu))
+    return lam, mu
+
+
+def _percentiles(lat):
+    a = np.sort(np.asarray(lat))
+    return float(np.percentile(a, 50)), float(np.percentile(a, 99))
+
+
+def bench_serve(ft, torch, lib, stream, args, local, dist):
+    import gc
+    t0 = time.perf_counter()
+    cases = serve_cases(ft, args.serve_meshes, device=local)
+    mesh_s = time.perf_counter() - t0
+    rng = np.random.default_rng(7)
+    payloads = _request_payloads(cases, rng)
+    t0 = time.perf_counter()
+    srv = ft.AssemblyServer(lanes=args.serve_lanes, max_jobs=16, device=local)
+    ids = []
+    for c in cases:
+        free, _ = srv.memory()
+        # admission: the pattern, values, slot maps and ring of the new mesh must fit
+        need = 40 * c["elements"] * (100 if c["type"] == "T10" else 8) * 3
+        if free < need:
+            break
+        ids.append(srv.add_mesh(c["form"], c["femm"], c["geom"], c["u"], c["cf"]))
+    cases = cases[:len(ids)]
+    setup_s = time.perf_counter() - t0
+    n = len(cases)
+    elems = np.array([c["elements"] for c in cases], dtype=np.float64)
+
+    def submit(k, kind, v):
+        mid = ids[k][0]
+        p = payloads[k]
+        return srv.submit_coef(mid, p["coef"][v]) if kind == 0 else \
+            srv.submit_coords(mid, p["coords"][v])
+
+    # capacity: every mesh re-assembled, all requests present at once
+    for rep in range(2):
+        srv.hold(True)
+        reqs = [submit(k, 0, rep % 2) for k in range(n)]
+        t0 = time.perf_counter()
+        srv.hold(False)
+        for r in reqs:
+            srv.wait(r)
+        burst_s = time.perf_counter() - t0
+    capacity = elems.sum() / burst_s                  # elements/s
+    mean_service = elems.mean() / capacity            # s per request at saturation
+    res = {"meshes": n, "elements": int(elems.sum()),
+           "types": {t: sum(1 for c in cases if c["type"] == t) for t in ("H8", "T10")},
+           "lanes": args.serve_lanes, "setup_s": {"meshes": mesh_s, "register": setup_s},
+           "capacity_elements_per_s": capacity, "sweep": []}
+    nreq = args.serve_requests
+    for frac in (0.3, 0.6, 0.9, 1.1):
+        rate = frac / mean_service                    # requests/s
+        arr = np.cumsum(rng.exponential(1.0 / rate, nreq))
+        which = rng.integers(0, n, nreq)
+        kinds = rng.integers(0, 2, nreq)
+        t_start = time.perf_counter()
+        reqs = []
+        for a, k, kd in zip(arr, which, kinds):
+            dt = t_start + a - time.perf_counter()
+            if dt > 0:
+                time.sleep(dt)
+            reqs.append(submit(int(k), int(kd), int(rng.integers(0, 2))))
+        lat = [srv.wait(r) for r in reqs]
+        span = time.perf_counter() - t_start
+        p50, p99 = _percentiles(lat)
+        res["sweep"].append({"load": frac, "rate_per_s": rate, "requests": nreq,
+                             "p50_ms": p50, "p99_ms": p99, "p99_over_p50": p99 / p50,
+                             "elements_per_s": float(elems[which].sum() / span)})
+    res["server"] = srv.stats()
+    srv.close()
+    # FP64: the same kind of stream served one request at a time by single calls
+    asm = ft.SysmatAssemblerGPU(precision="fp64", result="device", device=local)
+    mats = [_single_call_serve(ft, c, asm) for c in cases]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(n):
+        _fp64_request(ft, lib, cases[k], mats[k], payloads[k], 0, 0)
+    fp64_capacity = elems.sum() / (time.perf_counter() - t0)
+    rate = 0.6 * fp64_capacity / elems.mean()
+    nr = max(32, nreq // 2)
+    arr = np.cumsum(rng.exponential(1.0 / rate, nr))
+    which = rng.integers(0, n, nr)
+    kinds = rng.integers(0, 2, nr)
+    t_start = time.perf_counter()
+    lat = []
+    for a, k, kd in zip(arr, which, kinds):
+        dt = t_start + a - time.perf_counter()
+        if dt > 0:
+            time.sleep(dt)
+        _fp64_request(ft, lib, cases[int(k)], mats[int(k)], payloads[int(k)], int(kd), 1)
+        lat.append(1e3 * (time.perf_counter() - (t_start + a)))
+    p50, p99 = _percentiles(lat)
+    res["fp64_one_request_at_a_time"] = {"capacity_elements_per_s": fp64_capacity,
+                                         "load": 0.6, "p50_ms": p50, "p99_ms": p99,
+                                         "p99_over_p50": p99 / p50}
+    res["capacity_mixed_over_fp64"] = capacity / fp64_capacity
+    del mats, asm, srv, ids, cases
+    gc.collect()
+    torch.cuda.empty_cache()
+    return res
+
+
+def _single_call_serve(ft, c, asm):
+    if c["form"] == "diffusion":
+        return ft.bilform_diffusion(c["femm"], asm, c["geom"], c["u"], c["cf"])
+    return ft.bilform_lin_elastic(c["femm"], asm, c["geom"], c["u"], ft.DeforModelRed3D, c["cf"])
+
+
+def _fp64_request(ft, lib, c, K, payload, kind, v):
+    """One FP64 re-assembly through the C ABI: new coordinates or coefficients."""
+    L, nat = lib.L, lib.nat
+    if kind == 1:
+        x = payload["coords"][v]
+        nat.check(L.fegpu_femm_set_geometry(c["femm"]._h, 3, x.ctypes.data))
+        data = c["cf"].values if c["form"] == "diffusion" else c["cf"].lame
+    else:
+        data = payload["coef"][v]
+    if c["form"] == "diffusion":
+        coef = nat.Coef(nat.COEF_PER_ELEMENT, 1, data.ctypes.data)
+        nat.check(L.fegpu_bilform_diffusion(K.h, C.byref(coef), nat.FP64))
+    else:
+        coef = nat.Coef(nat.COEF_ISO_LAME, 2, data.ctypes.data)
+        nat.check(L.fegpu_bilform_lin_elastic(K.h, C.byref(coef), nat.FP64))
 
 
 def bench_h8(ft, torch, lib, stream, args, local, dist):
@@ -637,11 +842,16 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--headline-only", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--only", choices=["t10", "h20", "h8", "batch"], default=None,
+    ap.add_argument("--only", choices=["t10", "h20", "h8", "batch", "serve"], default=None,
                     help="run one workload only (profiling); prints its numbers")
     ap.add_argument("--h20-n", type=int, default=H20_N)
     ap.add_argument("--batch-meshes", type=int, default=256,
                     help="meshes of the mixed-type batch workload")
+    ap.add_argument("--serve-meshes", type=int, default=32,
+                    help="resident meshes of the serving workload")
+    ap.add_argument("--serve-requests", type=int, default=200,
+                    help="requests per load level of the serving sweep")
+    ap.add_argument("--serve-lanes", type=int, default=2)
     ap.add_argument("--t10-n", type=int, default=T10_N,
                     help="cells per side of the headline T10 block (60 = the benchmark size)")
     args = ap.parse_args()

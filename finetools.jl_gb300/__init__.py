@@ -10,8 +10,9 @@ package is the host-side mirror of the reference's Julia interface.
 """
 from ._native import FegpuError, load as load_library
 from .batch import AssemblyBatch
+from .serve import AssemblyServer
 from .assembly import (DeviceMatrix, SysmatAssemblerGPU, SysvecAssemblerGPU, assemble,
-                       makematrix, startassembly)
+                       conjugategradient, makematrix, startassembly)
 from .femm import (DataCache, DeforModelRed3D, ElementwiseData, FEMMBase, ForceIntensity,
                    IntegDomain, IsotropicElementwise, bilform_diffusion, bilform_dot,
                    bilform_lin_elastic, connectionmatrix, distribloads, innerproduct,

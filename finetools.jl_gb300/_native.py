@@ -17,6 +17,7 @@ Q4, H8, H20, T4, T10 = 0, 1, 2, 3, 4
 COEF_CONST, COEF_PER_ELEMENT, COEF_PER_QP, COEF_ISO_LAME = 0, 1, 2, 3
 FP64, MIXED = 0, 1
 FORM_DIFFUSION, FORM_LIN_ELASTIC, FORM_DOT = 0, 1, 2
+REQUEST_COEF, REQUEST_COORDS = 0, 1
 
 EXPORTS = [
     "fegpu_last_error", "fegpu_context_create", "fegpu_context_destroy",
@@ -26,12 +27,15 @@ EXPORTS = [
     "fegpu_dofmap_destroy", "fegpu_dofmap_copy_pattern", "fegpu_matrix_create",
     "fegpu_matrix_destroy", "fegpu_bilform_diffusion", "fegpu_bilform_lin_elastic",
     "fegpu_bilform_dot", "fegpu_linform_dot", "fegpu_matrix_nnz", "fegpu_matrix_copy_csc",
-    "fegpu_matrix_copy_values", "fegpu_matrix_spmv", "fegpu_assembler_create",
+    "fegpu_matrix_copy_values", "fegpu_matrix_spmv", "fegpu_matrix_cg", "fegpu_assembler_create",
     "fegpu_assembler_destroy", "fegpu_assembler_assemble", "fegpu_assembler_make",
     "fegpu_assembler_copy_csc", "fegpu_bilform_lin_elastic_noalloc",
     "fegpu_batch_create", "fegpu_batch_destroy", "fegpu_batch_add", "fegpu_batch_set_coef",
     "fegpu_batch_tune", "fegpu_batch_tile", "fegpu_batch_set_wait_limit", "fegpu_batch_launch",
     "fegpu_batch_wait", "fegpu_batch_run", "fegpu_batch_stats",
+    "fegpu_server_create", "fegpu_server_destroy", "fegpu_server_add_mesh", "fegpu_server_submit",
+    "fegpu_server_wait", "fegpu_server_drain", "fegpu_server_hold", "fegpu_server_stats",
+    "fegpu_server_memory",
 ]
 
 
@@ -83,6 +87,7 @@ def load(path: str = LIBPATH):
         "fegpu_matrix_copy_csc": ([vp, i32, vp, vp, vp], i32),
         "fegpu_matrix_copy_values": ([vp, vp], i32),
         "fegpu_matrix_spmv": ([vp, vp, vp], i32),
+        "fegpu_matrix_cg": ([vp, vp, vp, i32, vp], i32),
         "fegpu_assembler_create": ([vp, i32, i64, i64, pp], i32),
         "fegpu_assembler_destroy": ([vp], i32),
         "fegpu_assembler_assemble": ([vp, vp, i32, i32, vp, vp], i32),
@@ -100,6 +105,15 @@ def load(path: str = LIBPATH):
         "fegpu_batch_wait": ([vp], i32),
         "fegpu_batch_run": ([vp], i32),
         "fegpu_batch_stats": ([vp, p64, p64], i32),
+        "fegpu_server_create": ([vp, i32, i32, pp], i32),
+        "fegpu_server_destroy": ([vp], i32),
+        "fegpu_server_add_mesh": ([vp, vp, i32, C.POINTER(Coef), i32, p64], i32),
+        "fegpu_server_submit": ([vp, i64, i32, vp, i64, p64], i32),
+        "fegpu_server_wait": ([vp, i64, C.POINTER(C.c_double)], i32),
+        "fegpu_server_drain": ([vp], i32),
+        "fegpu_server_hold": ([vp, i32], i32),
+        "fegpu_server_stats": ([vp, p64, p64, p64], i32),
+        "fegpu_server_memory": ([vp, p64, p64], i32),
     }
     for name, (args, res) in proto.items():
         f = getattr(L, name)

@@ -46,6 +46,17 @@ class DeviceMatrix:
     def __matmul__(self, x):
         return self.spmv(x)
 
+    def cg(self, b, x0, maxiter):
+        """conjugategradient(K, b, x0, maxiter) on the device."""
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x0 = np.ascontiguousarray(x0, dtype=np.float64)
+        if b.shape != (self.shape[0],) or x0.shape != (self.shape[0],):
+            raise ValueError("Size mismatch")
+        x = np.empty_like(b)
+        nat.check(nat.load().fegpu_matrix_cg(self.h, nat.ptr(b), nat.ptr(x0), int(maxiter),
+                                             nat.ptr(x)))
+        return x
+
     def nnz(self, drop_zeros=None):
         dz = self.drop_zeros if drop_zeros is None else drop_zeros
         n = C.c_int64()
@@ -158,6 +169,15 @@ class SysvecAssemblerGPU:
         F = np.zeros(dm.ndof)
         nat.check(nat.load().fegpu_linform_dot(dm.h, C.byref(coef), m, nat.ptr(F)))
         return F
+
+
+def conjugategradient(A, b, x0, maxiter):
+    """conjugategradient (src/AlgoBaseModule.jl:425-445) for a matrix resident
+    on the GPU (a DeviceMatrix: ``SysmatAssemblerGPU(result="device")``)."""
+    if not isinstance(A, DeviceMatrix):
+        raise TypeError("conjugategradient runs on a DeviceMatrix (assemble with "
+                        "SysmatAssemblerGPU(result=\"device\")); there is no CPU path")
+    return A.cg(b, x0, maxiter)
 
 
 def startassembly(a, *args, **kw):

@@ -77,7 +77,8 @@ def build(jobs: int | None = None, verbose: bool = False, force: bool = False) -
             for log in ex.map(_compile, cmds):
                 if verbose and log:
                     sys.stderr.write(log)
-    if cmds or not os.path.exists(LIB):
+    if cmds or not os.path.exists(LIB) or any(
+            os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
         tmp = LIB + ".tmp"
         _compile([nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"])
         os.replace(tmp, LIB)

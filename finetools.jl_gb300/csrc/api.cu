@@ -83,9 +83,9 @@ int choose_tile(int etype, int form, int precision, int npts) {
   return te;
 }
 
-int mixed_tile_for(int etype, int npts) { return default_mixed_tile(etype, npts); }
-size_t mixed_smem_for(int etype, int npts, int te) {
-  return mixed_layout(nodes_per_elem(etype), manif_dim(etype), npts, te).total;
+int mixed_tile_for(int etype, int form, int npts) { return default_tile(etype, form, npts); }
+size_t mixed_smem_for(int etype, int form, int npts, int te) {
+  return tile_smem_bytes(etype, form, npts, te);
 }
 
 size_t form_smem_bytes(int etype, int form, int precision, int npts, int te) {
@@ -179,6 +179,13 @@ void stage_coef(fegpu_femm *fm, const fegpu_coef *cf, int expect_ncomp, KArgs &a
 
 }  // namespace
 
+void pack_geometry(const double *src_colmajor, int64_t nnodes, int sdim, double *xyz4,
+                   cudaStream_t s) {
+  if (nnodes <= 0) return;
+  k_pack_xyz<<<grid_of(nnodes), 256, 0, s>>>(src_colmajor, nnodes, sdim, xyz4);
+  FEGPU_CUDA(cudaGetLastError());
+}
+
 KArgs base_args(fegpu_matrix *K, fegpu_dofmap *dm) {
   fegpu_femm *fm = dm->femm;
   KArgs a;
@@ -234,8 +241,8 @@ void run_gather(fegpu_dofmap *dm, int form, KArgs &a) {
   const int bs = ndn * ndn, nblk = nne * (nne + 1) / 2;
   if (!dm->gather_ready) build_gather_plan(dm, nblk * bs);
   a.conn = fm->conn_orig.as<int32_t>();
-  a.te = default_mixed_tile(fm->etype, fm->npts);
-  FEGPU_REQUIRE(mixed_layout(nne, fm->mdim, fm->npts, a.te).total <= 227 * 1024,
+  a.te = default_tile(fm->etype, form, fm->npts);
+  FEGPU_REQUIRE(tile_smem_bytes(fm->etype, form, fm->npts, a.te) <= 227 * 1024,
                 "quadrature rule too large for the element kernel");
   GArgs g;
   g.n2e_ptr = dm->n2e_ptr.as<int64_t>();

@@ -28,45 +28,16 @@
 #include <string>
 #include <vector>
 
+#include "batch_host.h"
 #include "gather.cuh"
-#include "mixed.cuh"
+#include "mixed_fast.cuh"
 
 namespace fegpu {
 
-// job kinds the batch kernel is compiled for: element type x form x DOFs per node
-enum BatchCode {
-  BC_H8_DIFF, BC_H20_DIFF, BC_T4_DIFF, BC_T10_DIFF, BC_Q4_DIFF,
-  BC_H8_ELAST, BC_H20_ELAST, BC_T4_ELAST, BC_T10_ELAST,
-  BC_Q4_DOT1, BC_Q4_DOT3, BC_H8_DOT1, BC_H8_DOT3,
-  BC_COUNT
-};
-
-struct BatchJob {
-  KArgs k;
-  GArgs g;
-  int code;
-  int etype;
-  int ndn;
-  int64_t elem_floats;  // floats of one element's block set (upper node pairs)
-};
-
-struct BatchItem {
-  int job;
-  int kind;             // 0: element tile, 1: gather range
-  int64_t b, e;         // element range, or range of the job's gather order
-  int64_t chunk;        // element chunk (ring slot = chunk % ring)
-  int dep, dep_target;  // counter that must reach dep_target first (-1: none)
-  int done;             // counter incremented on completion
-};
-
 namespace {
 
-constexpr int kBatchThreads = kMixedThreads;
+static_assert(kBatchThreads == kMixedThreads, "element tiles fill the CTA");
 static_assert(kBatchThreads == 32 * kGatherWarps, "gather warps fill the CTA");
-constexpr int kGatherNodesPerItem = 64;
-// the scalar coefficient of a dot job is not folded into the point weight
-// (matrix coefficients travel in cab / cdiag)
-constexpr int kCoefNone = -1;
 
 __device__ __forceinline__ unsigned long long global_ns() {
   unsigned long long t;
@@ -92,19 +63,19 @@ __device__ void elem_dispatch(const BatchJob &J, int64_t b, int64_t e, int64_t c
   const int64_t e0 = chunk * J.g.chunk;
   const int ne = static_cast<int>(e - b);
   switch (J.code) {
-    case BC_H8_DIFF: mixed_tile<FEGPU_H8, F_DIFF_ISO, 1>(a, b, ne, smem, ke, e0); break;
-    case BC_H20_DIFF: mixed_tile<FEGPU_H20, F_DIFF_ISO, 1>(a, b, ne, smem, ke, e0); break;
-    case BC_T4_DIFF: mixed_tile<FEGPU_T4, F_DIFF_ISO, 1>(a, b, ne, smem, ke, e0); break;
-    case BC_T10_DIFF: mixed_tile<FEGPU_T10, F_DIFF_ISO, 1>(a, b, ne, smem, ke, e0); break;
-    case BC_Q4_DIFF: mixed_tile<FEGPU_Q4, F_DIFF_ISO, 1>(a, b, ne, smem, ke, e0); break;
-    case BC_H8_ELAST: mixed_tile<FEGPU_H8, F_ELAST_ISO, 3>(a, b, ne, smem, ke, e0); break;
-    case BC_H20_ELAST: mixed_tile<FEGPU_H20, F_ELAST_ISO, 3>(a, b, ne, smem, ke, e0); break;
-    case BC_T4_ELAST: mixed_tile<FEGPU_T4, F_ELAST_ISO, 3>(a, b, ne, smem, ke, e0); break;
-    case BC_T10_ELAST: mixed_tile<FEGPU_T10, F_ELAST_ISO, 3>(a, b, ne, smem, ke, e0); break;
-    case BC_Q4_DOT1: mixed_tile<FEGPU_Q4, F_DOT, 1>(a, b, ne, smem, ke, e0); break;
-    case BC_Q4_DOT3: mixed_tile<FEGPU_Q4, F_DOT, 3>(a, b, ne, smem, ke, e0); break;
-    case BC_H8_DOT1: mixed_tile<FEGPU_H8, F_DOT, 1>(a, b, ne, smem, ke, e0); break;
-    case BC_H8_DOT3: mixed_tile<FEGPU_H8, F_DOT, 3>(a, b, ne, smem, ke, e0); break;
+    case BC_H8_DIFF: mixed_tile_fast<FEGPU_H8, F_DIFF_ISO, 1>(a, b, ne, smem, ke, e0); break;
+    case BC_H20_DIFF: mixed_tile_fast<FEGPU_H20, F_DIFF_ISO, 1>(a, b, ne, smem, ke, e0); break;
+    case BC_T4_DIFF: mixed_tile_fast<FEGPU_T4, F_DIFF_ISO, 1>(a, b, ne, smem, ke, e0); break;
+    case BC_T10_DIFF: mixed_tile_fast<FEGPU_T10, F_DIFF_ISO, 1>(a, b, ne, smem, ke, e0); break;
+    case BC_Q4_DIFF: mixed_tile_fast<FEGPU_Q4, F_DIFF_ISO, 1>(a, b, ne, smem, ke, e0); break;
+    case BC_H8_ELAST: mixed_tile_fast<FEGPU_H8, F_ELAST_ISO, 3>(a, b, ne, smem, ke, e0); break;
+    case BC_H20_ELAST: mixed_tile_fast<FEGPU_H20, F_ELAST_ISO, 3>(a, b, ne, smem, ke, e0); break;
+    case BC_T4_ELAST: mixed_tile_fast<FEGPU_T4, F_ELAST_ISO, 3>(a, b, ne, smem, ke, e0); break;
+    case BC_T10_ELAST: mixed_tile_fast<FEGPU_T10, F_ELAST_ISO, 3>(a, b, ne, smem, ke, e0); break;
+    case BC_Q4_DOT1: mixed_tile_fast<FEGPU_Q4, F_DOT, 1>(a, b, ne, smem, ke, e0); break;
+    case BC_Q4_DOT3: mixed_tile_fast<FEGPU_Q4, F_DOT, 3>(a, b, ne, smem, ke, e0); break;
+    case BC_H8_DOT1: mixed_tile_fast<FEGPU_H8, F_DOT, 1>(a, b, ne, smem, ke, e0); break;
+    case BC_H8_DOT3: mixed_tile_fast<FEGPU_H8, F_DOT, 3>(a, b, ne, smem, ke, e0); break;
     default: break;
   }
 }
@@ -145,12 +116,14 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch(const BatchJob *jobs,
     const BatchItem I = items[it];
     if (threadIdx.x == 0) {
       int go = *reinterpret_cast<volatile int *>(status) == 0;
-      if (go && I.dep >= 0) {
-        const volatile int *ctr = counters + I.dep;
-        if (*ctr < I.dep_target) {
+      for (int d = 0; d < 2 && go; ++d) {
+        if (I.dep[d] < 0) continue;
+        const volatile int *ctr = counters + I.dep[d];
+        const int target = I.target[d];
+        if (*ctr < target) {
           const unsigned long long t0 = global_ns();
           long long spins = 0;
-          while (*ctr < I.dep_target) {
+          while (*ctr < target) {
             __nanosleep(128);
             if ((++spins & 255) != 0) continue;
             if (*reinterpret_cast<volatile int *>(status) != 0) {  // another wait gave up
@@ -165,8 +138,8 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch(const BatchJob *jobs,
             }
           }
         }
-        __threadfence();  // acquire: the producers' blocks are visible
       }
+      __threadfence();  // acquire: the producers' writes are visible
       s_go = go;
     }
     __syncthreads();
@@ -182,6 +155,8 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch(const BatchJob *jobs,
     }
   }
 }
+
+}  // namespace
 
 int batch_code(int etype, int form, int ndn) {
   if (form == F_DIFF_ISO && ndn == 1) {
@@ -206,12 +181,50 @@ int batch_code(int etype, int form, int ndn) {
   return -1;
 }
 
-const char *const kCodeNames[BC_COUNT] = {
+static const char *const kCodeNames[BC_COUNT] = {
     "H8_diffusion",  "H20_diffusion", "T4_diffusion", "T10_diffusion", "Q4_diffusion",
     "H8_elasticity", "H20_elasticity", "T4_elasticity", "T10_elasticity",
     "Q4_dot1",       "Q4_dot3",        "H8_dot1",      "H8_dot3"};
 
-}  // namespace
+const char *batch_code_name(int code) {
+  return code >= 0 && code < BC_COUNT ? kCodeNames[code] : "unknown";
+}
+
+void launch_batch_kernel(int grid, size_t smem, cudaStream_t s, const BatchJob *jobs,
+                         const BatchItem *items, int nitems, int *next, int *counters,
+                         int *status, double wait_s) {
+  k_batch<<<grid, kBatchThreads, smem, s>>>(jobs, items, nitems, next, counters, status,
+                                            static_cast<unsigned long long>(wait_s * 1e9));
+  FEGPU_CUDA(cudaGetLastError());
+}
+
+int batch_grid(int num_sms, size_t smem, int nitems, double share) {
+  // always the same (maximal) limit, so threads launching concurrently with
+  // different needs cannot undercut each other's launches
+  FEGPU_REQUIRE(smem <= kBatchMaxSmem, "batch: shared-memory need too large");
+  FEGPU_CUDA(cudaFuncSetAttribute(k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  static_cast<int>(kBatchMaxSmem)));
+  int per_sm = 0;
+  FEGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch, kBatchThreads, smem));
+  per_sm = std::max(per_sm, 1);
+  const int full = num_sms * per_sm;
+  const int g = static_cast<int>(full * std::min(1.0, std::max(share, 0.0)));
+  return std::max(1, std::min(nitems, std::max(g, 1)));
+}
+
+size_t batch_smem_bytes(const std::vector<BatchJob> &jobs,
+                        const std::vector<const fegpu_dofmap *> &dms) {
+  size_t smem = 0;
+  for (size_t j = 0; j < jobs.size(); ++j) {
+    const fegpu_femm *fm = dms[j]->femm;
+    smem = std::max(smem, tile_smem_bytes(fm->etype, jobs[j].form, fm->npts, jobs[j].k.te));
+    smem = std::max(smem, sizeof(float) * gather_warp_stride(jobs[j].ndn, jobs[j].g.maxdeg) *
+                              kGatherWarps);
+  }
+  FEGPU_REQUIRE(smem <= kBatchMaxSmem, "batch: shared-memory need above the per-CTA limit");
+  return smem;
+}
+
 }  // namespace fegpu
 
 using namespace fegpu;
@@ -241,20 +254,10 @@ struct fegpu_batch {
 };
 
 namespace fegpu {
-namespace {
 
-void drop_graph(fegpu_batch *b) {
-  if (b->exec) cudaGraphExecDestroy(b->exec);
-  if (b->graph) cudaGraphDestroy(b->graph);
-  b->exec = nullptr;
-  b->graph = nullptr;
-}
-
-// Kernel arguments of one job from its matrix, form and coefficient.  The
-// coefficient values are copied to a buffer owned by the job (element order).
-void fill_job(fegpu_batch *b, size_t index, const fegpu_coef *cf) {
-  fegpu_batch::Job &J = b->jobs[index];
-  fegpu_matrix *K = J.K;
+// ---- job descriptors ----------------------------------------------------------
+void make_batch_job(fegpu_matrix *K, int form, int code, int m, const fegpu_coef *cf, int te,
+                    std::unique_ptr<DevBuf> &coef, float *ring, cudaStream_t s, BatchJob &out) {
   fegpu_dofmap *dm = K->dm;
   fegpu_femm *fm = dm->femm;
   const int nne = fm->nne, ndn = dm->ndn;
@@ -262,11 +265,11 @@ void fill_job(fegpu_batch *b, size_t index, const fegpu_coef *cf) {
   if (!dm->gather_ready) build_gather_plan(dm, static_cast<int>(elem_floats));
   KArgs a = base_args(K, dm);
   a.conn = fm->conn_orig.as<int32_t>();
-  a.measure_m = J.m;
+  a.measure_m = m;
   a.coef_kind = cf->kind;
   a.ncomp = cf->ncomp;
   int64_t width = 0;  // coefficient values per element
-  if (J.form == F_ELAST_ISO) {
+  if (form == F_ELAST_ISO) {
     if (cf->kind == FEGPU_COEF_CONST) {
       double lam, mu;
       FEGPU_REQUIRE(cf->ncomp == 36 && is_isotropic(cf->data, lam, mu),
@@ -282,13 +285,13 @@ void fill_job(fegpu_batch *b, size_t index, const fegpu_coef *cf) {
     FEGPU_REQUIRE(cf->kind == FEGPU_COEF_CONST || cf->kind == FEGPU_COEF_PER_ELEMENT ||
                       cf->kind == FEGPU_COEF_PER_QP,
                   "batch: bad coefficient kind");
-    const bool matrix_coef = J.form == F_DOT && ndn > 1 && cf->ncomp == ndn * ndn;
+    const bool matrix_coef = form == F_DOT && ndn > 1 && cf->ncomp == ndn * ndn;
     FEGPU_REQUIRE(cf->ncomp == 1 || (matrix_coef && cf->kind == FEGPU_COEF_CONST),
                   "batch: scalar coefficients (or a constant ndn x ndn matrix for dot)");
     if (cf->kind == FEGPU_COEF_CONST) a.cconst[0] = cf->data[0];
     if (cf->kind == FEGPU_COEF_PER_ELEMENT) width = 1;
     if (cf->kind == FEGPU_COEF_PER_QP) width = fm->npts;
-    if (J.form == F_DOT) {
+    if (form == F_DOT) {
       // element-matrix entry (k,p),(l,q) = N_k N_l c[p][q] (src/FEMMBaseModule.jl:1357-1361),
       // arranged as the symmetric assembler keeps it (lower triangle, mirrored)
       double c[9] = {0};
@@ -307,19 +310,18 @@ void fill_job(fegpu_batch *b, size_t index, const fegpu_coef *cf) {
   }
   if (width > 0) {
     const int64_t n = width * fm->nelem;
-    if (!J.coef) J.coef = std::make_unique<DevBuf>();
-    J.coef->alloc(sizeof(double) * std::max<int64_t>(n, 1));
-    if (n > 0)
-      FEGPU_CUDA(cudaMemcpyAsync(J.coef->p, cf->data, sizeof(double) * n, cudaMemcpyHostToDevice,
-                                 b->ctx->stream));
-    a.coef = J.coef->as<double>();
+    if (!coef) coef = std::make_unique<DevBuf>();
+    coef->alloc(sizeof(double) * std::max<int64_t>(n, 1));
+    if (n > 0 && cf->data)
+      FEGPU_CUDA(cudaMemcpyAsync(coef->p, cf->data, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    a.coef = coef->as<double>();
   } else {
     a.coef = nullptr;
   }
-  a.te = b->tile.count(J.code) ? b->tile[J.code] : mixed_tile_for(fm->etype, fm->npts);
+  a.te = te > 0 ? te : mixed_tile_for(fm->etype, form, fm->npts);
   a.ke = nullptr;
-  J.d.k = a;
-  GArgs &g = J.d.g;
+  out.k = a;
+  GArgs &g = out.g;
   std::memset(&g, 0, sizeof(g));
   g.n2e_ptr = dm->n2e_ptr.as<int64_t>();
   g.n2e_elem = dm->n2e_elem.as<int32_t>();
@@ -328,14 +330,7 @@ void fill_job(fegpu_batch *b, size_t index, const fegpu_coef *cf) {
   g.nodes = dm->gnodes.as<int32_t>();
   g.nptr = dm->nptr.as<int64_t>();
   g.pos = dm->pos_orig.as<uint16_t>();
-  g.ke = dm->ke.as<float>();
-  for (size_t j = 0; j < index; ++j)
-    if (b->jobs[j].K->dm == dm) {  // the dofmap's ring is taken: use a private one
-      if (!J.ring) J.ring = std::make_unique<DevBuf>();
-      J.ring->alloc(dm->ke.bytes);
-      g.ke = J.ring->as<float>();
-      break;
-    }
+  g.ke = ring ? ring : dm->ke.as<float>();
   g.chunk = dm->chunk;
   g.ring = dm->ring;
   g.dof = dm->dof.as<int32_t>();
@@ -344,97 +339,54 @@ void fill_job(fegpu_batch *b, size_t index, const fegpu_coef *cf) {
   g.cpoff = dm->contiguous ? nullptr : dm->cpoff.as<int64_t>();
   g.val = K->val.as<double>();
   g.maxdeg = dm->maxdeg;
-  J.d.code = J.code;
-  J.d.etype = fm->etype;
-  J.d.ndn = ndn;
-  J.d.elem_floats = elem_floats;
+  out.code = code;
+  out.form = form;
+  out.etype = fm->etype;
+  out.ndn = ndn;
+  out.elem_floats = elem_floats;
 }
 
-// Work queue.  Jobs pass through a window: each round emits the next stage
-// of every job in the window, and a job that has emitted its last stage
-// leaves it for the next waiting job.  While a stage of one job waits for
-// its predecessor, the CTAs work on the other jobs' stages; and the window is
-// kept to the jobs whose live element blocks (the chunk being written and the
-// one being gathered) fit in about half of the L2 cache, so blocks are read
-// back from L2 rather than from HBM.
+namespace {
+
+void drop_graph(fegpu_batch *b) {
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  b->exec = nullptr;
+  b->graph = nullptr;
+}
+
+// (Re)build a job's descriptor: coefficient copy and private ring as needed.
+void fill_job(fegpu_batch *b, size_t index, const fegpu_coef *cf) {
+  fegpu_batch::Job &J = b->jobs[index];
+  fegpu_dofmap *dm = J.K->dm;
+  const int nne = dm->femm->nne, ndn = dm->ndn;
+  const int64_t elem_floats = static_cast<int64_t>(nne) * (nne + 1) / 2 * ndn * ndn;
+  if (!dm->gather_ready) build_gather_plan(dm, static_cast<int>(elem_floats));
+  float *ring = nullptr;
+  for (size_t j = 0; j < index; ++j)
+    if (b->jobs[j].K->dm == dm) {  // the dofmap's ring is taken: use a private one
+      if (!J.ring) J.ring = std::make_unique<DevBuf>();
+      J.ring->alloc(dm->ke.bytes);
+      ring = J.ring->as<float>();
+      break;
+    }
+  const int te = b->tile.count(J.code) ? b->tile[J.code] : 0;
+  make_batch_job(J.K, J.form, J.code, J.m, cf, te, J.coef, ring, b->ctx->stream, J.d);
+}
+
 void build_queue(fegpu_batch *b) {
-  const size_t njobs = b->jobs.size();
-  std::vector<BatchItem> items;
-  std::vector<int> stage_base(njobs), nstage(njobs);
-  int ncount = 0;
-  for (size_t j = 0; j < njobs; ++j) {
-    const fegpu_dofmap *dm = b->jobs[j].K->dm;
-    nstage[j] = static_cast<int>(2 * (static_cast<int64_t>(dm->chunk_nodes.size()) - 1));
-    stage_base[j] = ncount;
-    ncount += nstage[j];
-  }
-  std::vector<int> stage_items(std::max(ncount, 1), 0);
-  auto emit = [&](size_t j, int s) {
-    const auto &J = b->jobs[j];
-    const fegpu_dofmap *dm = J.K->dm;
-    const int64_t c = s / 2;
-    const int ctr = stage_base[j] + s;
-    const int dep = s > 0 ? ctr - 1 : -1;
-    const int target = s > 0 ? stage_items[ctr - 1] : 0;
-    auto push = [&](int kind, int64_t x0, int64_t x1) {
-      items.push_back(BatchItem{static_cast<int>(j), kind, x0, x1, c, dep, target, ctr});
-      stage_items[ctr]++;
-    };
-    if (s % 2 == 0) {
-      const int64_t e0 = c * dm->chunk, e1 = std::min(dm->femm->nelem, (c + 1) * dm->chunk);
-      for (int64_t x = e0; x < e1; x += J.d.k.te) push(0, x, std::min(e1, x + J.d.k.te));
-      if (e0 >= e1) push(0, e0, e0);
-    } else {
-      const int64_t n0 = dm->chunk_nodes[c], n1 = dm->chunk_nodes[c + 1];
-      for (int64_t x = n0; x < n1; x += kGatherNodesPerItem)
-        push(1, x, std::min(n1, x + kGatherNodesPerItem));
-      if (n0 >= n1) push(1, n0, n0);  // a stage without nodes still completes
-    }
-  };
-  auto live_bytes = [&](size_t j) {
-    const auto &J = b->jobs[j];
-    const int64_t e = std::min<int64_t>(J.K->dm->chunk, J.K->dm->femm->nelem);
-    return static_cast<size_t>(2 * e * J.d.elem_floats * sizeof(float));
-  };
-  const size_t budget = 64u << 20;
-  std::vector<size_t> window;
-  std::vector<int> next_stage(njobs, 0);
-  size_t admitted = 0, live = 0;
-  auto admit = [&]() {
-    while (admitted < njobs &&
-           (window.size() < 2 || live + live_bytes(admitted) <= budget)) {
-      if (nstage[admitted] > 0) {
-        window.push_back(admitted);
-        live += live_bytes(admitted);
-      }
-      ++admitted;
-    }
-  };
-  admit();
-  while (!window.empty()) {
-    std::vector<size_t> keep;
-    for (size_t j : window) {
-      emit(j, next_stage[j]++);
-      if (next_stage[j] < nstage[j]) keep.push_back(j);
-      else live -= live_bytes(j);
-    }
-    window.swap(keep);
-    admit();
-  }
-  FEGPU_REQUIRE(items.size() < (1u << 31), "batch: too many work items");
-  size_t smem = 0;
   std::vector<BatchJob> dj;
+  std::vector<const fegpu_dofmap *> dms;
   for (auto &J : b->jobs) {
     dj.push_back(J.d);
-    const fegpu_femm *fm = J.K->dm->femm;
-    smem = std::max(smem, mixed_layout(fm->nne, fm->mdim, fm->npts, J.d.k.te).total);
-    smem = std::max(smem, sizeof(float) * gather_warp_stride(J.d.ndn, J.d.g.maxdeg) * kGatherWarps);
+    dms.push_back(J.K->dm);
   }
-  FEGPU_REQUIRE(smem <= 227 * 1024, "batch: shared-memory need above 227 KB");
+  std::vector<BatchItem> items;
+  const int ncount = build_batch_items(dj, dms, 64u << 20, items);
+  b->smem = batch_smem_bytes(dj, dms);
   cudaStream_t st = b->ctx->stream;
   b->nitems = static_cast<int>(items.size());
-  b->ncounters = std::max(ncount, 1);
-  b->smem = smem;
+  b->ncounters = ncount;
   b->d_items.alloc(sizeof(BatchItem) * std::max<size_t>(items.size(), 1));
   if (!items.empty())
     FEGPU_CUDA(cudaMemcpyAsync(b->d_items.p, items.data(), sizeof(BatchItem) * items.size(),
@@ -446,12 +398,7 @@ void build_queue(fegpu_batch *b) {
   b->d_counters.alloc(sizeof(int) * b->ncounters);
   b->d_next.alloc(sizeof(int));
   b->d_status.alloc(sizeof(int));
-  FEGPU_CUDA(cudaFuncSetAttribute(k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  static_cast<int>(smem)));
-  int per_sm = 0;
-  FEGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch, kBatchThreads, smem));
-  per_sm = std::max(per_sm, 1);
-  b->grid = std::max(1, std::min(b->nitems, b->ctx->num_sms * per_sm));
+  b->grid = batch_grid(b->ctx->num_sms, b->smem, b->nitems, 1.0);
   FEGPU_CUDA(cudaStreamSynchronize(st));
   b->dirty = false;
 }
@@ -461,11 +408,9 @@ void enqueue_batch(fegpu_batch *b, cudaStream_t st) {
   FEGPU_CUDA(cudaMemsetAsync(b->d_counters.p, 0, sizeof(int) * b->ncounters, st));
   FEGPU_CUDA(cudaMemsetAsync(b->d_next.p, 0, sizeof(int), st));
   FEGPU_CUDA(cudaMemsetAsync(b->d_status.p, 0, sizeof(int), st));
-  k_batch<<<b->grid, kBatchThreads, b->smem, st>>>(
-      b->d_jobs.as<BatchJob>(), b->d_items.as<BatchItem>(), b->nitems, b->d_next.as<int>(),
-      b->d_counters.as<int>(), b->d_status.as<int>(),
-      static_cast<unsigned long long>(b->wait_s * 1e9));
-  FEGPU_CUDA(cudaGetLastError());
+  launch_batch_kernel(b->grid, b->smem, st, b->d_jobs.as<BatchJob>(), b->d_items.as<BatchItem>(),
+                      b->nitems, b->d_next.as<int>(), b->d_counters.as<int>(),
+                      b->d_status.as<int>(), b->wait_s);
 }
 
 void check_status(fegpu_batch *b) {
@@ -662,7 +607,8 @@ int fegpu_batch_tune(fegpu_batch *b, const char *cache_path) {
         int te;
         while (std::fscanf(f, "%63s %d", name, &te) == 2)
           for (int c = 0; c < BC_COUNT; ++c)
-            if (std::strcmp(name, kCodeNames[c]) == 0 && te > 0 && te <= 4096) b->tile[c] = te;
+            if (std::strcmp(name, batch_code_name(c)) == 0 && te > 0 && te <= 4096)
+              b->tile[c] = te;
         std::fclose(f);
       }
     }
@@ -686,7 +632,7 @@ int fegpu_batch_tune(fegpu_batch *b, const char *cache_path) {
         float best = 3.0e38f;
         int best_te = J.d.k.te;
         for (int te : cands) {
-          if (mixed_layout(fm->nne, fm->mdim, fm->npts, te).total > 112 * 1024) break;
+          if (tile_smem_bytes(fm->etype, J.form, fm->npts, te) > 112 * 1024) break;
           fegpu_batch one;
           one.ctx = b->ctx;
           fegpu_batch::Job S;
@@ -716,7 +662,7 @@ int fegpu_batch_tune(fegpu_batch *b, const char *cache_path) {
         b->tile[J.code] = best_te;
         if (cache_path) {
           if (FILE *f = std::fopen(cache_path, "a")) {
-            std::fprintf(f, "%s %d\n", kCodeNames[J.code], best_te);
+            std::fprintf(f, "%s %d\n", batch_code_name(J.code), best_te);
             std::fclose(f);
           }
         }

@@ -127,6 +127,7 @@ struct fegpu_dofmap {
   bool gather_ready = false;
   int64_t chunk = 0;        // elements per chunk of the block ring
   int ring = 0;             // chunks held by the ring
+  int span = 0;             // max chunk distance between a node's first and last element
   std::vector<int64_t> chunk_nodes;  // gather node ranges per chunk
   fegpu::DevBuf n2e_ptr;    // int64 [nnodes + 1]
   fegpu::DevBuf n2e_elem;   // int32: incident elements, increasing
@@ -226,8 +227,13 @@ int launch_gather(int etype, int ndn, const GArgs &g, int num_sms, cudaStream_t 
 // (g.n2e_slot unused)
 int launch_gather_inline_slot(int etype, int ndn, const GArgs &g, int num_sms, cudaStream_t s);
 int launch_mixed(int etype, int form, const KArgs &a, int sms, cudaStream_t s);
-int mixed_tile_for(int etype, int npts);
-size_t mixed_smem_for(int etype, int npts, int te);
+// elements per tile and the tile's shared memory for a form of the mixed path
+int mixed_tile_for(int etype, int form, int npts);
+size_t mixed_smem_for(int etype, int form, int npts, int te);
+
+// Node coordinates: column-major nnodes x sdim (device) -> [nnodes][4] (device).
+void pack_geometry(const double *src_colmajor, int64_t nnodes, int sdim, double *xyz4,
+                   cudaStream_t s);
 
 // ---- shared by the entry points -----------------------------------------------------
 KArgs base_args(fegpu_matrix *K, fegpu_dofmap *dm);

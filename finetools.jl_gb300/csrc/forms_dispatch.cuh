@@ -4,7 +4,7 @@
 #pragma once
 
 #include "elements.cuh"
-#include "mixed.cuh"
+#include "mixed_fast.cuh"
 
 namespace fegpu {
 

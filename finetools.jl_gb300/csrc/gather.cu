@@ -140,7 +140,10 @@ void build_gather_plan(fegpu_dofmap *dm, int block_values) {
     if (ptr[n + 1] == ptr[n]) continue;
     order[at[elem[ptr[n + 1] - 1] / dm->chunk]++] = static_cast<int32_t>(n);
   }
-  dm->ring = static_cast<int>(std::min<int64_t>(span + 1, nch));
+  // ring: the chunks a gather reads (span + 1) plus one, so the element tiles
+  // of the next chunk can be written while a gather still reads the ring
+  dm->span = static_cast<int>(span);
+  dm->ring = static_cast<int>(std::min<int64_t>(span + 2, nch));
   for (size_t q = 0; q < elem.size(); ++q) {
     const int64_t ce = elem[q] / dm->chunk;
     slot[q] = static_cast<int32_t>((ce % dm->ring) * dm->chunk + (elem[q] - ce * dm->chunk));

@@ -34,8 +34,10 @@ __device__ __forceinline__ void two_sum_acc(float &h, float &l, float v) {
 // h, l is first renormalised so that |l| <= ulp(h)/2; the exact sum is then
 // formed as a 64-bit fixed-point integer aligned 37 bits below h's leading
 // bit (bits of l further down are truncated: < 2^-60 relative), normalised
-// and rounded to 53 bits (nearest, ties to even).
-__device__ __forceinline__ double ff_to_double(float h, float l) {
+// and rounded to 53 bits (nearest, ties to even).  General case; the row
+// gather uses ff_to_double below, which calls this one for the rare inputs
+// outside its fast path.
+static __device__ __noinline__ double ff_to_double_exact(float h, float l) {
   const float s = __fadd_rn(h, l);
   l = __fsub_rn(l, __fsub_rn(s, h));
   h = s;
@@ -81,6 +83,36 @@ __device__ __forceinline__ double ff_to_double(float h, float l) {
 }
 
 
+// (h + l) as an FP64 value, integer arithmetic only, for the common case of
+// a normal h and |l| <= ulp(h)/2 (after renormalisation): h's 24-bit
+// mantissa is placed in the 53-bit mantissa of the result and l is added at
+// its position, 2^(29 - d) units of the result's last place with d the
+// exponent difference (d >= 24); bits of l below the result's last place are
+// truncated (faithful: error < 1 ulp of FP64).  Other inputs (zero,
+// subnormal, inf/nan, |l| not small against h) take ff_to_double_exact.
+__device__ __forceinline__ double ff_to_double(float h, float l) {
+  const float s = __fadd_rn(h, l);
+  l = __fsub_rn(l, __fsub_rn(s, h));
+  h = s;
+  const uint32_t hb = __float_as_uint(h), lb = __float_as_uint(l);
+  const uint32_t eh = (hb >> 23) & 0xffu, el = (lb >> 23) & 0xffu;
+  const int d = static_cast<int>(eh) - static_cast<int>(el);
+  if (eh == 0u || eh == 0xffu || (el != 0u && d < 24)) return ff_to_double_exact(h, l);
+  uint64_t M = static_cast<uint64_t>((hb & 0x7fffffu) | 0x800000u) << 29;
+  if (el != 0u && d < 61) {
+    const uint32_t ml = (lb & 0x7fffffu) | 0x800000u;
+    const uint32_t c = d <= 29 ? (ml << (29 - d)) : (ml >> (d - 29));
+    M = ((lb ^ hb) >> 31) ? M - c : M + c;
+  }
+  uint64_t E = static_cast<uint64_t>(eh) + 896u;
+  if (M < (1ull << 52)) {  // h a power of two, l of the other sign
+    M <<= 1;
+    E -= 1u;
+  }
+  return __longlong_as_double(static_cast<long long>(
+      (static_cast<uint64_t>(hb >> 31) << 63) | (E << 52) | (M & ((1ull << 52) - 1ull))));
+}
+
 // One warp gathers the rows of node A: accumulators hi/lo (NDN x cmax floats
 // each, in the warp's shared region), blocks of the incident elements in
 // element order, then one FP64 store per CSR value of the node's rows.
@@ -91,6 +123,8 @@ __device__ __forceinline__ void gather_node(const GArgs &g, int32_t A, float *hi
                                             int lane) {
   constexpr int NBLK = NNE * (NNE + 1) / 2;
   constexpr int BS = NDN * NDN;
+  constexpr int NTASK = NNE * NDN;  // (b, j): node of the element, column component
+  constexpr int NSLOT = (NTASK + 31) / 32;
   const int cmax = g.maxdeg * NDN;
   const int cols = static_cast<int>(g.nptr[A + 1] - g.nptr[A]) * NDN;
   {
@@ -98,6 +132,15 @@ __device__ __forceinline__ void gather_node(const GArgs &g, int32_t A, float *hi
     const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
     for (int c = lane; c < (2 * NDN * cmax) / 4; c += 32) z[c] = zero;
     for (int c = ((2 * NDN * cmax) / 4) * 4 + lane; c < 2 * NDN * cmax; c += 32) hi[c] = 0.f;
+  }
+  // the lane's (b, j) tasks, fixed for all incident elements
+  int tb[NSLOT], tj[NSLOT], trow[NSLOT];
+#pragma unroll
+  for (int s = 0; s < NSLOT; ++s) {
+    const int task = min(lane + 32 * s, NTASK - 1);
+    tb[s] = task / NDN;
+    tj[s] = task - tb[s] * NDN;
+    trow[s] = tb[s] * NNE - tb[s] * (tb[s] - 1) / 2 - tb[s];  // pair(b, x) = trow + x, x >= b
   }
   __syncwarp();
   for (int64_t q = g.n2e_ptr[A]; q < g.n2e_ptr[A + 1]; ++q) {
@@ -113,22 +156,20 @@ __device__ __forceinline__ void gather_node(const GArgs &g, int32_t A, float *hi
     }
     const float *kb = g.ke + slot * NBLK * BS;
     const uint16_t *pe = g.pos + (e * NNE + a) * NNE;
-    for (int task = lane; task < NNE * NDN; task += 32) {
-      const int b = task / NDN, j = task - (task / NDN) * NDN;
+    const int rowa = a * NNE - a * (a - 1) / 2 - a;
+#pragma unroll
+    for (int s = 0; s < NSLOT; ++s) {
+      if (lane + 32 * s >= NTASK) break;
+      const int b = tb[s], j = tj[s];
+      const bool up = a <= b;  // block (a, b) stored; else (b, a), transposed
+      const float *blk = kb + (up ? rowa + b : trow[s] + a) * BS + (up ? j : j * NDN);
+      const int step = up ? NDN : 1;
       const int col = pe[b] * NDN + j;
-      if (a <= b) {
-        const float *blk = kb + (a * NNE - a * (a - 1) / 2 + (b - a)) * BS;
+      float v[NDN];
 #pragma unroll
-        for (int i = 0; i < NDN; ++i)
-          two_sum_acc(hi[i * cmax + col], lo[i * cmax + col],
-                      L2ONLY ? __ldcg(blk + i * NDN + j) : blk[i * NDN + j]);
-      } else {
-        const float *blk = kb + (b * NNE - b * (b - 1) / 2 + (a - b)) * BS;
+      for (int i = 0; i < NDN; ++i) v[i] = L2ONLY ? __ldcg(blk + i * step) : blk[i * step];
 #pragma unroll
-        for (int i = 0; i < NDN; ++i)
-          two_sum_acc(hi[i * cmax + col], lo[i * cmax + col],
-                      L2ONLY ? __ldcg(blk + j * NDN + i) : blk[j * NDN + i]);
-      }
+      for (int i = 0; i < NDN; ++i) two_sum_acc(hi[i * cmax + col], lo[i * cmax + col], v[i]);
     }
     __syncwarp();
   }

@@ -400,49 +400,4 @@ __device__ __forceinline__ void mixed_tile(const KArgs &a, int64_t eb, int ne,
   }
 }
 
-template <int ET, int FORM, int NDN>
-__global__ void __launch_bounds__(kMixedThreads) k_blocks_mixed(const KArgs a) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const int64_t nel = a.e1 - a.e0;
-  const int64_t ntiles = (nel + a.te - 1) / a.te;
-  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const int64_t eb = a.e0 + tile * a.te;
-    const int ne = static_cast<int>(min(static_cast<int64_t>(a.te), a.e1 - eb));
-    mixed_tile<ET, FORM, NDN>(a, eb, ne, smem, a.ke, a.e0);
-  }
-}
-
-// Elements per tile: enough Gram tasks for two passes of the CTA, within a
-// shared-memory budget that leaves two CTAs per SM.
-inline int default_mixed_tile(int etype, int npts) {
-  const int nne = nodes_per_elem(etype), mdim = manif_dim(etype);
-  const size_t budget = 72 * 1024;
-  const MixedLayout one = mixed_layout(nne, mdim, npts, 1);
-  const MixedLayout two = mixed_layout(nne, mdim, npts, 2);
-  const size_t per = two.total - one.total;
-  const size_t fixed = one.total - per;
-  const int fit = static_cast<int>((budget - std::min(budget, fixed)) / per);
-  const int want = (kMixedThreads + mixed_groups(nne) - 1) / mixed_groups(nne);
-  return std::max(1, std::min(fit, want));
-}
-
-template <int ET, int FORM, int NDN>
-int launch_blocks_mixed_t(const KArgs &a, int num_sms, cudaStream_t s) {
-  constexpr int NNE = ElemT<ET>::NNE, MDIM = ElemT<ET>::MDIM;
-  const MixedLayout L = mixed_layout(NNE, MDIM, a.npts, a.te);
-  auto kern = k_blocks_mixed<ET, FORM, NDN>;
-  FEGPU_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  static_cast<int>(L.total)));
-  int per_sm = 0;
-  FEGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kMixedThreads, L.total));
-  per_sm = std::max(per_sm, 1);
-  const int64_t nel = a.e1 - a.e0;
-  if (nel <= 0) return 0;
-  const int64_t ntiles = (nel + a.te - 1) / a.te;
-  const int grid = static_cast<int>(std::min<int64_t>(ntiles, static_cast<int64_t>(num_sms) * per_sm));
-  kern<<<grid, kMixedThreads, L.total, s>>>(a);
-  FEGPU_CUDA(cudaGetLastError());
-  return 1;
-}
-
 }  // namespace fegpu

@@ -166,8 +166,8 @@ extern "C" int fegpu_bilform_lin_elastic_noalloc(fegpu_matrix *K, const fegpu_co
     }
 
     a.conn = fm->conn_orig.as<int32_t>();
-    a.te = mixed_tile_for(fm->etype, fm->npts);
-    FEGPU_REQUIRE(mixed_smem_for(fm->etype, fm->npts, a.te) <= 227 * 1024,
+    a.te = mixed_tile_for(fm->etype, form, fm->npts);
+    FEGPU_REQUIRE(mixed_smem_for(fm->etype, form, fm->npts, a.te) <= 227 * 1024,
                   "quadrature rule too large for the element kernel");
     GArgs g;
     g.n2e_ptr = dm->n2e_ptr.as<int64_t>();

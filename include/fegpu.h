@@ -160,6 +160,11 @@ int fegpu_matrix_copy_csc(fegpu_matrix *K, int drop_zeros, int64_t *colptr,
 int fegpu_matrix_copy_values(fegpu_matrix *K, double *nzval);
 /* y = K x on the device (host vectors of length nalldofs) */
 int fegpu_matrix_spmv(fegpu_matrix *K, const double *x, double *y);
+/* conjugategradient(K, b, x0, maxiter) (src/AlgoBaseModule.jl:425-445): the
+ * reference's iteration, every step on the device; host vectors of length
+ * nalldofs; the result goes to x. */
+int fegpu_matrix_cg(fegpu_matrix *K, const double *b, const double *x0, int maxiter,
+                    double *x);
 
 /* Allocation-free mixed-precision bilform_lin_elastic.  No counterpart in the
  * reference: it serves callers that cannot allocate device memory once they
@@ -217,6 +222,44 @@ int fegpu_batch_launch(fegpu_batch *b);
 int fegpu_batch_wait(fegpu_batch *b);
 int fegpu_batch_run(fegpu_batch *b);
 int fegpu_batch_stats(fegpu_batch *b, int64_t *jobs, int64_t *items);
+
+/* ---- serving loop: re-assembly requests on resident meshes -----------------
+ * No reference counterpart (the reference assembles on demand, one call per
+ * matrix): a server keeps meshes resident on the device -- the handles of a
+ * matrix (femm, dofmap, matrix) plus its form and coefficient, registered once
+ * -- and accepts requests that carry new per-element coefficients
+ * (FEGPU_REQUEST_COEF: the same layout as the coefficient the mesh was added
+ * with) or new node coordinates (FEGPU_REQUEST_COORDS: nnodes x sdim,
+ * column-major, as geom.values).  A worker thread batches pending requests
+ * (the oldest of every mesh not already on the GPU, up to max_jobs) into
+ * launches of the persistent kernel on `lanes` streams, each lane using
+ * 1/lanes of the GPU, so batches formed while others run overlap them.
+ * Requests of one mesh complete in submission order; a request's result is
+ * the mesh's matrix (values on the device, read with fegpu_matrix_copy_values
+ * before the mesh's next request completes).  Every request is evaluated as
+ * the batch path (FEGPU_MIXED); results do not depend on what else is in the
+ * batch.  Latency = completion (host callback behind the kernel) - submit.
+ * The data passed to fegpu_server_submit is copied; the matrices must outlive
+ * the server; a coordinates request also changes the femm's geometry. */
+#define FEGPU_REQUEST_COEF 0
+#define FEGPU_REQUEST_COORDS 1
+typedef struct fegpu_server fegpu_server;
+int fegpu_server_create(fegpu_context *ctx, int lanes, int max_jobs, fegpu_server **out);
+int fegpu_server_destroy(fegpu_server *s);
+int fegpu_server_add_mesh(fegpu_server *s, fegpu_matrix *K, int form, const fegpu_coef *cf,
+                          int m, int64_t *mesh_id);
+int fegpu_server_submit(fegpu_server *s, int64_t mesh_id, int kind, const double *data,
+                        int64_t count, int64_t *request_id);
+/* blocks until the request completed; its latency in ms; collects it */
+int fegpu_server_wait(fegpu_server *s, int64_t request_id, double *latency_ms);
+/* blocks until no request is pending or running */
+int fegpu_server_drain(fegpu_server *s);
+/* hold = 1: no new launches (requests accumulate, e.g. during maintenance or
+ * to admit a burst at once); hold = 0: resume */
+int fegpu_server_hold(fegpu_server *s, int hold);
+int fegpu_server_stats(fegpu_server *s, int64_t *batches, int64_t *jobs, int64_t *pending);
+/* free and total device memory (admission of new meshes) */
+int fegpu_server_memory(fegpu_server *s, int64_t *free_bytes, int64_t *total_bytes);
 
 /* ---- generic assembler for element matrices formed on the host -----------
  * startassembly! / assemble! / makematrix! of SysmatAssemblerSparse(Symm)

@@ -314,3 +314,21 @@ def linform_dot(etype, conn, xyz, dofnums, nalldofs, pc, w, force, coef_kind=COE
     if lib().orc_linform_dot(C.byref(P), C.byref(Cf), m, _p(F)) != 0:
         raise ValueError(_err())
     return F
+
+
+def conjugategradient(A, b, x0, maxiter):
+    """conjugategradient (src/AlgoBaseModule.jl:425-445), restated in numpy:
+    the same iteration (two products with A per step); A any matrix numpy or
+    scipy can multiply."""
+    x = np.array(x0, dtype=np.float64, copy=True)
+    gt = A @ x - b                          # transpose of the gradient
+    d = gt.copy()
+    for _ in range(maxiter):
+        Ad = A @ d
+        rho = float(d @ Ad)
+        alpha = -float(gt @ d) / rho
+        x += alpha * d
+        gt = A @ x - b
+        beta = float(gt @ Ad) / rho
+        d = beta * d - gt
+    return x

@@ -222,10 +222,22 @@ def coloring_and_pattern():
     return out
 
 
+def cg_case():
+    """The system of the conjugategradient test (test/test_miscellaneous.jl,
+    module mconjugategradient1): A, b, x0 = 0 and maxiter."""
+    rel = "test/test_miscellaneous.jl"
+    txt, line = module_text(read(rel), "mconjugategradient1", rel)
+    A, _ = parse_matrix(txt, txt.index("[", re.search(r"A\s*=", txt).end()))
+    b, _ = parse_matrix(txt, txt.index("[", re.search(r"\bb\s*=", txt).end()))
+    maxiter = int(re.search(r"maxiter\s*=\s*(\d+)", txt).group(1))
+    return {"source": f"{rel}:{line}", "A": A, "b": [r[0] for r in b], "maxiter": maxiter}
+
+
 def main():
     if not os.path.isdir(REF):
         sys.exit(f"reference sources not found at {REF}")
-    data = {"assembler": assembler_kats(), "patch": patch_tests(), **coloring_and_pattern()}
+    data = {"assembler": assembler_kats(), "patch": patch_tests(), **coloring_and_pattern(),
+            "conjugategradient": cg_case()}
     with open(OUT, "w") as f:
         json.dump(data, f, indent=1)
     print("wrote", OUT)

@@ -1,0 +1,133 @@
+"""Serving loop (fegpu_server_*): re-assembly requests on resident meshes.
+
+Bar: a request's matrix equals the single-call FEGPU_MIXED assembly with the
+request's data bit for bit, whether the request ran alone or batched with
+others; requests of one mesh complete in submission order; coordinate
+updates move the mesh.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _field(ft, n, ndn):
+    return ft.numberdofs(ft.NodalField(np.zeros((n, ndn))))
+
+
+def _meshes(ft, seed=6):
+    rng = np.random.default_rng(seed)
+    out = []
+    for i, (et, n) in enumerate([("H8", 3000), ("T10", 4000), ("H8", 800), ("T10", 1500),
+                                 ("H20", 600), ("T4", 2000)]):
+        fens, fes = ft.nearest_block(et, n, seed=100 + i)
+        E = fes.count()
+        rule = {"H8": ft.GaussRule(3, 2), "H20": ft.GaussRule(3, 3), "T4": ft.TetRule(1),
+                "T10": ft.TetRule(4)}[et]
+        femm = ft.FEMMBase(ft.IntegDomain(fes, rule))
+        geom = ft.NodalField(fens.xyz)
+        if i % 2 == 0:
+            form, ndn = "diffusion", 1
+            cf = ft.ElementwiseData(rng.lognormal(0.0, 1.0, E))
+        else:
+            form, ndn = "lin_elastic", 3
+            cf = ft.IsotropicElementwise(rng.lognormal(np.log(70e9), 1.0, E), np.full(E, 0.3))
+        out.append(dict(form=form, femm=femm, geom=geom, u=_field(ft, fens.count(), ndn), cf=cf,
+                        fens=fens, E=E))
+    return out
+
+
+def _new_coef(ft, c, rng):
+    if c["form"] == "diffusion":
+        cf = ft.ElementwiseData(rng.lognormal(0.0, 1.0, c["E"]))
+        return cf, cf.values
+    cf = ft.IsotropicElementwise(rng.lognormal(np.log(70e9), 1.0, c["E"]), np.full(c["E"], 0.3))
+    return cf, cf.lame
+
+
+def _single_mixed(ft, c, cf, geom=None):
+    asm = ft.SysmatAssemblerGPU(precision="mixed", result="device")
+    g = geom if geom is not None else c["geom"]
+    if c["form"] == "diffusion":
+        return ft.bilform_diffusion(c["femm"], asm, g, c["u"], cf).values()
+    return ft.bilform_lin_elastic(c["femm"], asm, g, c["u"], ft.DeforModelRed3D, cf).values()
+
+
+def test_requests_in_the_mix_equal_single_calls(ft):
+    cases = _meshes(ft)
+    srv = ft.AssemblyServer(lanes=2, max_jobs=4)
+    ids = [srv.add_mesh(c["form"], c["femm"], c["geom"], c["u"], c["cf"]) for c in cases]
+    rng = np.random.default_rng(9)
+    reqs, cfs = [], []
+    srv.hold(True)                               # a burst, admitted at once
+    for (mid, _), c in zip(ids, cases):
+        cf, data = _new_coef(ft, c, rng)
+        cfs.append(cf)
+        reqs.append(srv.submit_coef(mid, data))
+    srv.hold(False)
+    lat = [srv.wait(r) for r in reqs]
+    assert all(x > 0 for x in lat)
+    st = srv.stats()
+    # 6 requests, at most 4 per launch, 2 lanes: two launches of 4 + 2 jobs
+    assert st["jobs"] == len(cases) and st["batches"] == 2
+    mixed = [M.values() for _, M in ids]
+    srv.close()
+    for v, c, cf in zip(mixed, cases, cfs):
+        assert np.array_equal(v, _single_mixed(ft, c, cf))
+    # the same requests alone (one per launch)
+    srv1 = ft.AssemblyServer(lanes=1, max_jobs=1)
+    for (mid0, _), c, cf, v in zip(ids, cases, cfs, mixed):
+        mid, M = srv1.add_mesh(c["form"], c["femm"], c["geom"], c["u"], c["cf"])
+        data = cf.values if c["form"] == "diffusion" else cf.lame
+        srv1.wait(srv1.submit_coef(mid, data))
+        assert np.array_equal(M.values(), v)
+    srv1.close()
+
+
+def test_requests_of_one_mesh_complete_in_order(ft):
+    c = _meshes(ft)[1]
+    srv = ft.AssemblyServer(lanes=3, max_jobs=8)
+    mid, M = srv.add_mesh(c["form"], c["femm"], c["geom"], c["u"], c["cf"])
+    rng = np.random.default_rng(2)
+    cfs, reqs = [], []
+    for _ in range(4):
+        cf, data = _new_coef(ft, c, rng)
+        cfs.append(cf)
+        reqs.append(srv.submit_coef(mid, data))
+    srv.drain()
+    lat = [srv.wait(r) for r in reqs]
+    # submitted back to back and served one at a time: latencies grow
+    assert all(b >= a for a, b in zip(lat, lat[1:]))
+    got = M.values()
+    srv.close()
+    assert np.array_equal(got, _single_mixed(ft, c, cfs[-1]))
+
+
+def test_coordinate_update(ft):
+    c = _meshes(ft)[3]
+    srv = ft.AssemblyServer(lanes=2)
+    mid, M = srv.add_mesh(c["form"], c["femm"], c["geom"], c["u"], c["cf"])
+    rng = np.random.default_rng(5)
+    xyz = c["geom"].values.copy()
+    inside = np.all((xyz > 1e-9) & (xyz < 1 - 1e-9), axis=1)
+    xyz[inside] += rng.uniform(-0.002, 0.002, (inside.sum(), 3))
+    srv.wait(srv.submit_coords(mid, xyz))
+    got = M.values()
+    srv.close()
+    assert np.array_equal(got, _single_mixed(ft, c, c["cf"], geom=ft.NodalField(xyz)))
+
+
+def test_server_rejects_bad_requests(ft):
+    c = _meshes(ft)[0]
+    srv = ft.AssemblyServer()
+    mid, _ = srv.add_mesh(c["form"], c["femm"], c["geom"], c["u"], c["cf"])
+    with pytest.raises(ft.FegpuError, match="Size mismatch"):
+        srv.submit_coef(mid, np.ones(c["E"] + 1))
+    with pytest.raises(ft.FegpuError, match="no such mesh"):
+        srv.submit_coef(mid + 5, np.ones(c["E"]))
+    mid2, _ = srv.add_mesh("diffusion", c["femm"], c["geom"], c["u"], ft.DataCache(1.0))
+    with pytest.raises(ft.FegpuError, match="constant coefficient"):
+        srv.submit_coef(mid2, np.ones(c["E"]))
+    free, total = srv.memory()
+    assert 0 < free <= total
+    srv.close()

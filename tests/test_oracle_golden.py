@@ -221,3 +221,13 @@ def test_element_kernels_vs_dense(O):
     ref = np.zeros((8, 8))
     ref[np.ix_(conn[0] - 1, conn[0] - 1)] = loc
     assert np.linalg.norm(K - ref) / np.linalg.norm(ref) <= 1e-9
+
+
+def test_conjugategradient_on_reference_system(O, kats):
+    """The system of the reference's conjugategradient test: 20 iterations on
+    the 6x6 Lehmer matrix reach the solution."""
+    c = kats["conjugategradient"]
+    A, b = np.array(c["A"]), np.array(c["b"])
+    x = O.conjugategradient(A, b, np.zeros(len(b)), c["maxiter"])
+    assert np.linalg.norm(A @ x - b) <= 1e-12 * np.linalg.norm(b)
+    assert np.allclose(x, np.linalg.solve(A, b), rtol=1e-10, atol=1e-12)
