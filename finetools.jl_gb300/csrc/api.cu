@@ -7,6 +7,7 @@
 // are asynchronous with respect to the host; every copy-out synchronises.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <new>
@@ -80,6 +81,17 @@ int choose_tile(int etype, int form, int precision, int npts) {
   int te = static_cast<int>((budget - std::min(budget, fixed)) / std::max<size_t>(per, 1));
   const int want = std::max(1, (2 * kFormThreads + npts - 1) / npts);
   te = std::max(1, std::min(te, want));
+  // FEGPU_FP64_TILE overrides the elements per tile of the FP64 colour
+  // kernels (tuning; capped by the shared memory of one CTA)
+  if (precision == FEGPU_FP64) {
+    if (const char *env = std::getenv("FEGPU_FP64_TILE")) {
+      const int v = std::atoi(env);
+      if (v > 0) {
+        te = v;
+        while (te > 1 && smem_layout(nne, mdim, npts, te, tsize, grad).total > 227 * 1024) --te;
+      }
+    }
+  }
   return te;
 }
 
@@ -262,15 +274,38 @@ void run_gather(fegpu_dofmap *dm, int form, KArgs &a) {
   g.val = a.val;
   g.maxdeg = dm->maxdeg;
   const int64_t nch = static_cast<int64_t>(dm->chunk_nodes.size()) - 1;
-  if (ctx->timing) FEGPU_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
+  // Element blocks on the side stream, gathers on the context stream: the
+  // blocks of chunk c wait for the gather that last read their ring slot
+  // (G(c - ring + span)) and for everything before this call; the gather of
+  // chunk c waits for the blocks of chunk c.  Events are kept per ring slot.
+  cudaStream_t s0 = ctx->stream;
+  if (!ctx->side) FEGPU_CUDA(cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking));
+  while (static_cast<int>(ctx->ev_blocks.size()) < dm->ring) {
+    cudaEvent_t e1, e2;
+    FEGPU_CUDA(cudaEventCreateWithFlags(&e1, cudaEventDisableTiming));
+    FEGPU_CUDA(cudaEventCreateWithFlags(&e2, cudaEventDisableTiming));
+    ctx->ev_blocks.push_back(e1);
+    ctx->ev_gather.push_back(e2);
+  }
+  if (ctx->timing) FEGPU_CUDA(cudaEventRecord(ctx->ev0, s0));
+  FEGPU_CUDA(cudaEventRecord(ctx->ev_gather[0], s0));  // work before this call
+  FEGPU_CUDA(cudaStreamWaitEvent(ctx->side, ctx->ev_gather[0], 0));
   for (int64_t c = 0; c < nch; ++c) {
+    const int slot = static_cast<int>(c % dm->ring);
+    if (c >= dm->ring) {
+      const int64_t reader = c - dm->ring + dm->span;  // last gather reading the slot
+      FEGPU_CUDA(cudaStreamWaitEvent(ctx->side, ctx->ev_gather[reader % dm->ring], 0));
+    }
     a.e0 = c * dm->chunk;
     a.e1 = std::min(fm->nelem, (c + 1) * dm->chunk);
-    a.ke = dm->ke.as<float>() + (c % dm->ring) * dm->chunk * nblk * bs;
-    ctx->launches += launch_mixed(fm->etype, form, a, ctx->num_sms, ctx->stream);
+    a.ke = dm->ke.as<float>() + slot * dm->chunk * nblk * bs;
+    ctx->launches += launch_mixed(fm->etype, form, a, ctx->num_sms, ctx->side);
+    FEGPU_CUDA(cudaEventRecord(ctx->ev_blocks[slot], ctx->side));
+    FEGPU_CUDA(cudaStreamWaitEvent(s0, ctx->ev_blocks[slot], 0));
     g.n0 = dm->chunk_nodes[c];
     g.n1 = dm->chunk_nodes[c + 1];
-    ctx->launches += launch_gather(fm->etype, ndn, g, ctx->num_sms, ctx->stream);
+    ctx->launches += launch_gather(fm->etype, ndn, g, ctx->num_sms, s0);
+    FEGPU_CUDA(cudaEventRecord(ctx->ev_gather[slot], s0));
   }
   if (ctx->timing) {
     FEGPU_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
@@ -377,6 +412,9 @@ int fegpu_context_destroy(fegpu_context *ctx) {
     cudaStreamSynchronize(ctx->stream);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    for (cudaEvent_t e : ctx->ev_blocks) cudaEventDestroy(e);
+    for (cudaEvent_t e : ctx->ev_gather) cudaEventDestroy(e);
+    if (ctx->side) cudaStreamDestroy(ctx->side);
     ctx->scratch.release();
     ctx->scratch2.release();
     cudaStreamDestroy(ctx->stream);

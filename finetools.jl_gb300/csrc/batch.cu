@@ -101,7 +101,7 @@ __device__ void gather_dispatch(const BatchJob &J, int64_t b, int64_t e, unsigne
 }
 
 // The persistent kernel.  status: 0 ok, 1 a wait ran out of time.
-__global__ void __launch_bounds__(kBatchThreads) k_batch(const BatchJob *jobs,
+__global__ void __launch_bounds__(kBatchThreads, 2) k_batch(const BatchJob *jobs,
                                                          const BatchItem *items, int nitems,
                                                          int *next, int *counters, int *status,
                                                          unsigned long long wait_ns) {
@@ -318,7 +318,7 @@ void make_batch_job(fegpu_matrix *K, int form, int code, int m, const fegpu_coef
   } else {
     a.coef = nullptr;
   }
-  a.te = te > 0 ? te : mixed_tile_for(fm->etype, form, fm->npts);
+  a.te = te > 0 ? std::min(te, max_fast_tile(fm->etype)) : mixed_tile_for(fm->etype, form, fm->npts);
   a.ke = nullptr;
   out.k = a;
   GArgs &g = out.g;
@@ -632,7 +632,9 @@ int fegpu_batch_tune(fegpu_batch *b, const char *cache_path) {
         float best = 3.0e38f;
         int best_te = J.d.k.te;
         for (int te : cands) {
-          if (tile_smem_bytes(fm->etype, J.form, fm->npts, te) > 112 * 1024) break;
+          if (te > max_fast_tile(fm->etype) ||
+              tile_smem_bytes(fm->etype, J.form, fm->npts, te) > 112 * 1024)
+            break;
           fegpu_batch one;
           one.ctx = b->ctx;
           fegpu_batch::Job S;

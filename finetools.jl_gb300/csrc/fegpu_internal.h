@@ -91,6 +91,10 @@ struct fegpu_context {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double kernel_ms = 0.0;   // accumulated element-kernel time
   int64_t launches = 0;     // kernels launched by the library
+  // mixed path: a second stream for the element blocks, so chunk c+1's blocks
+  // overlap chunk c's gather; events per ring slot order them (created on use)
+  cudaStream_t side = nullptr;
+  std::vector<cudaEvent_t> ev_blocks, ev_gather;
 };
 
 struct fegpu_femm {

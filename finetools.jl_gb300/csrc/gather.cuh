@@ -9,6 +9,7 @@
 #include <cstdint>
 
 #include "fegpu_internal.h"
+#include "ffconv.h"
 
 namespace fegpu {
 
@@ -28,89 +29,6 @@ __device__ __forceinline__ void two_sum_acc(float &h, float &l, float v) {
   const float err = __fadd_rn(__fsub_rn(h, __fsub_rn(s, bb)), __fsub_rn(v, bb));
   h = s;
   l = __fadd_rn(l, err);
-}
-
-// (h + l) rounded to FP64 using integer arithmetic only (no FP64 pipe).
-// h, l is first renormalised so that |l| <= ulp(h)/2; the exact sum is then
-// formed as a 64-bit fixed-point integer aligned 37 bits below h's leading
-// bit (bits of l further down are truncated: < 2^-60 relative), normalised
-// and rounded to 53 bits (nearest, ties to even).  General case; the row
-// gather uses ff_to_double below, which calls this one for the rare inputs
-// outside its fast path.
-static __device__ __noinline__ double ff_to_double_exact(float h, float l) {
-  const float s = __fadd_rn(h, l);
-  l = __fsub_rn(l, __fsub_rn(s, h));
-  h = s;
-  const uint32_t hb = __float_as_uint(h);
-  const uint32_t eh = (hb >> 23) & 0xffu;
-  if (eh == 0u) {
-    // zero (or an FP32-subnormal sum, below 1.2e-38): signed zero
-    return __longlong_as_double(static_cast<long long>(static_cast<uint64_t>(hb >> 31) << 63));
-  }
-  if (eh == 0xffu) {  // inf / nan keep their class
-    const uint64_t nanbit = (hb & 0x7fffffu) ? (1ull << 51) : 0ull;
-    return __longlong_as_double(static_cast<long long>(
-        (static_cast<uint64_t>(hb >> 31) << 63) | (0x7ffull << 52) | nanbit));
-  }
-  const uint64_t mh = static_cast<uint64_t>((hb & 0x7fffffu) | 0x800000u);
-  uint64_t H = mh << 37;
-  const uint32_t lb = __float_as_uint(l);
-  const uint32_t el = (lb >> 23) & 0xffu;
-  if (el != 0u && el != 0xffu) {
-    const uint64_t ml = static_cast<uint64_t>((lb & 0x7fffffu) | 0x800000u);
-    const int d = static_cast<int>(eh) - static_cast<int>(el);
-    uint64_t L = 0;
-    if (d <= 37) L = ml << (37 - d);
-    else if (d < 37 + 24) L = ml >> (d - 37);
-    if ((lb >> 31) == (hb >> 31)) H += L;
-    else H -= L;
-  }
-  const int p = 63 - __clzll(static_cast<long long>(H));  // 59..61
-  const int drop = p - 52;
-  uint64_t mant = H >> drop;
-  const uint64_t rem = H & ((1ull << drop) - 1ull);
-  const uint64_t half = 1ull << (drop - 1);
-  if (rem > half || (rem == half && (mant & 1ull))) ++mant;
-  int p2 = p;
-  if (mant >> 53) {
-    mant >>= 1;
-    ++p2;
-  }
-  const uint64_t E = static_cast<uint64_t>(p2 + static_cast<int>(eh) + 836);
-  const uint64_t bits = (static_cast<uint64_t>(hb >> 31) << 63) | (E << 52) |
-                        (mant & ((1ull << 52) - 1ull));
-  return __longlong_as_double(static_cast<long long>(bits));
-}
-
-
-// (h + l) as an FP64 value, integer arithmetic only, for the common case of
-// a normal h and |l| <= ulp(h)/2 (after renormalisation): h's 24-bit
-// mantissa is placed in the 53-bit mantissa of the result and l is added at
-// its position, 2^(29 - d) units of the result's last place with d the
-// exponent difference (d >= 24); bits of l below the result's last place are
-// truncated (faithful: error < 1 ulp of FP64).  Other inputs (zero,
-// subnormal, inf/nan, |l| not small against h) take ff_to_double_exact.
-__device__ __forceinline__ double ff_to_double(float h, float l) {
-  const float s = __fadd_rn(h, l);
-  l = __fsub_rn(l, __fsub_rn(s, h));
-  h = s;
-  const uint32_t hb = __float_as_uint(h), lb = __float_as_uint(l);
-  const uint32_t eh = (hb >> 23) & 0xffu, el = (lb >> 23) & 0xffu;
-  const int d = static_cast<int>(eh) - static_cast<int>(el);
-  if (eh == 0u || eh == 0xffu || (el != 0u && d < 24)) return ff_to_double_exact(h, l);
-  uint64_t M = static_cast<uint64_t>((hb & 0x7fffffu) | 0x800000u) << 29;
-  if (el != 0u && d < 61) {
-    const uint32_t ml = (lb & 0x7fffffu) | 0x800000u;
-    const uint32_t c = d <= 29 ? (ml << (29 - d)) : (ml >> (d - 29));
-    M = ((lb ^ hb) >> 31) ? M - c : M + c;
-  }
-  uint64_t E = static_cast<uint64_t>(eh) + 896u;
-  if (M < (1ull << 52)) {  // h a power of two, l of the other sign
-    M <<= 1;
-    E -= 1u;
-  }
-  return __longlong_as_double(static_cast<long long>(
-      (static_cast<uint64_t>(hb >> 31) << 63) | (E << 52) | (M & ((1ull << 52) - 1ull))));
 }
 
 // One warp gathers the rows of node A: accumulators hi/lo (NDN x cmax floats

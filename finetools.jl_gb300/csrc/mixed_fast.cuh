@@ -43,10 +43,12 @@ __host__ __device__ constexpr int fast_slot(int b) { return b + b / 8; }
 __host__ __device__ constexpr int fast_stride(int nne) { return fast_slot(nne - 1) + 1; }
 
 struct FastLayout {
-  size_t conn, fx, jinv, det, w, lame, g, total;
+  size_t conn, fx, jinv, det, w, lame, g, stage, total;
 };
 
-__host__ __device__ inline FastLayout fast_layout(int nne, int npts, int te) {
+// stage: the tile's blocks before the coalesced copy to the ring; it overlays
+// the gradients (dead by then) and extends past them when larger.
+__host__ __device__ inline FastLayout fast_layout(int nne, int npts, int te, int ndn = 3) {
   FastLayout L;
   size_t o = 0;
   L.conn = o;
@@ -64,7 +66,10 @@ __host__ __device__ inline FastLayout fast_layout(int nne, int npts, int te) {
   o += sizeof(float) * te * 2;
   o = align_up(o, 16);
   L.g = o;
-  o += sizeof(float4) * te * npts * fast_stride(nne);
+  L.stage = o;
+  const size_t gbytes = sizeof(float4) * te * npts * fast_stride(nne);
+  const size_t sbytes = sizeof(float) * te * (nne * (nne + 1) / 2) * ndn * ndn;
+  o += gbytes > sbytes ? gbytes : sbytes;
   L.total = align_up(o, 16);
   return L;
 }
@@ -74,10 +79,12 @@ __host__ __device__ constexpr int fast_tiles_for(int nne) {
   return nne >= 20 ? FastTiles<20>::NT
                    : (nne >= 10 ? FastTiles<10>::NT : (nne >= 8 ? FastTiles<8>::NT : FastTiles<4>::NT));
 }
-inline int default_fast_tile(int etype) {
+// the largest tile: one (element, node-pair tile) task per thread
+inline int max_fast_tile(int etype) {
   const int nt = fast_tiles_for(nodes_per_elem(etype));
-  return std::max(1, 256 / nt);
+  return std::max(1, kMixedThreads / nt);
 }
+inline int default_fast_tile(int etype) { return max_fast_tile(etype); }
 
 template <int ET, int FORM, int NDN>
 __device__ __forceinline__ void mixed_tile_fast(const KArgs &a, int64_t eb, int ne,
@@ -91,7 +98,7 @@ __device__ __forceinline__ void mixed_tile_fast(const KArgs &a, int64_t eb, int 
   constexpr int TA = T::TA, TB = T::TB, NT = T::NT;
   static_assert(FORM == F_DIFF_ISO || FORM == F_ELAST_ISO || FORM == F_DOT, "isotropic forms");
   const int npts = a.npts, te = a.te;
-  const FastLayout L = fast_layout(NNE, npts, te);
+  const FastLayout L = fast_layout(NNE, npts, te, NDN);
   const float *fN = a.tab32;
   const float *fdN = a.tab32 + npts * NNE;
   const float *fw = fdN + npts * NNE * MDIM;
@@ -222,29 +229,40 @@ __device__ __forceinline__ void mixed_tile_fast(const KArgs &a, int64_t eb, int 
     sW[i] = w;
   }
   __syncthreads();
-  // C. (g, w) per (element, point, node)
+  // C. (g, w) per (element, point, node): thread t handles node t % NNE of
+  // the (element, point) rows t / NNE, t / NNE + R, ... (R = threads / NNE)
   if constexpr (GRAD) {
-    for (int i = tid; i < ne * npts * NNE; i += nth) {
-      const int eq = i / NNE, k = i - eq * NNE;
-      const int q = eq - (eq / npts) * npts;
-      const float *inv = sJinv + eq * 9;
-      const float *d = fdN + (q * NNE + k) * MDIM;
-      float g[3] = {0.f, 0.f, 0.f};
+    const int R = nth / NNE;
+    const int k = tid % NNE, r0 = tid / NNE;
+    if (r0 < R) {
+      int q = r0 % npts;
+      const int qstep = R % npts;
+      for (int eq = r0; eq < ne * npts; eq += R) {
+        const float *inv = sJinv + eq * 9;
+        const float *d = fdN + (q * NNE + k) * MDIM;
+        float g[3] = {0.f, 0.f, 0.f};
 #pragma unroll
-      for (int c = 0; c < MDIM; ++c) {
-        float v = 0.f;
+        for (int c = 0; c < MDIM; ++c) {
+          float v = 0.f;
 #pragma unroll
-        for (int m = 0; m < MDIM; ++m) v = fmaf(d[m], inv[m * 3 + c], v);
-        g[c] = v;
+          for (int m = 0; m < MDIM; ++m) v = fmaf(d[m], inv[m * 3 + c], v);
+          g[c] = v;
+        }
+        sG[eq * SLOTS + fast_slot(k)] = make_float4(g[0], g[1], g[2], sW[eq]);
+        q += qstep;
+        if (q >= npts) q -= npts;
       }
-      sG[eq * SLOTS + fast_slot(k)] = make_float4(g[0], g[1], g[2], sW[eq]);
     }
     __syncthreads();
   }
-  // D. Gram sums per (element, tile of node pairs), form map, block stores
-  for (int i = tid; i < ne * NT; i += nth) {
-    const int e = i / NT;
-    int t = i - e * NT, A = 0, B = 0;
+  // D. Gram sums per (element, tile of node pairs), form map, block stores.
+  // One task per thread (te * NT <= threads): the staging barrier below is
+  // reached by every thread.
+  {
+    const int i = tid;
+    const bool active = i < ne * NT;
+    const int e = active ? i / NT : 0;
+    int t = active ? i - e * NT : 0, A = 0, B = 0;
     {
       int n = 0;
       bool found = false;
@@ -276,7 +294,7 @@ __device__ __forceinline__ void mixed_tile_fast(const KArgs &a, int64_t eb, int 
         for (int r = 0; r < NM; ++r) M[u][v][r] = 0.f;
     if constexpr (GRAD) {
       const float4 *G = sG + static_cast<size_t>(e) * npts * SLOTS;
-      for (int q = 0; q < npts; ++q) {
+      for (int q = 0; q < (active ? npts : 0); ++q) {
         const float4 *Gq = G + q * SLOTS;
         float wa[TA][3];
 #pragma unroll
@@ -309,7 +327,7 @@ __device__ __forceinline__ void mixed_tile_fast(const KArgs &a, int64_t eb, int 
       }
     } else {
       // dot: s_ab = sum_q w N_a N_b (src/FEMMBaseModule.jl:1357-1361)
-      for (int q = 0; q < npts; ++q) {
+      for (int q = 0; q < (active ? npts : 0); ++q) {
         const float w = sW[e * npts + q];
         float wn[TA];
 #pragma unroll
@@ -327,14 +345,18 @@ __device__ __forceinline__ void mixed_tile_fast(const KArgs &a, int64_t eb, int 
       lam = sLame[2 * e];
       mu = sLame[2 * e + 1];
     }
-    float *kb = ke + static_cast<int64_t>(eb + e - e0) * NBLK * BS;
+    // blocks go to a staging copy of the tile's ring segment in shared memory
+    // (over the gradients, once every thread is done with them), then out
+    // with coalesced stores
+    __syncthreads();
+    float *kb = reinterpret_cast<float *>(smem + L.stage) + static_cast<int64_t>(e) * NBLK * BS;
 #pragma unroll
     for (int u = 0; u < TA; ++u) {
       const int pa = TA * A + u;
 #pragma unroll
       for (int v = 0; v < TB; ++v) {
         const int pb = TB * B + v;
-        if (pa >= NNE || pb >= NNE || pb < pa) continue;
+        if (!active || pa >= NNE || pb >= NNE || pb < pa) continue;
         float *out = kb + (pa * NNE - pa * (pa - 1) / 2 + (pb - pa)) * BS;
         if constexpr (FORM == F_DIFF_ISO) {
           out[0] = M[u][v][0];
@@ -367,6 +389,19 @@ __device__ __forceinline__ void mixed_tile_fast(const KArgs &a, int64_t eb, int 
       }
     }
   }
+  __syncthreads();
+  {
+    const int64_t nfl = static_cast<int64_t>(ne) * NBLK * BS;
+    const float *src = reinterpret_cast<const float *>(smem + L.stage);
+    float *dst = ke + static_cast<int64_t>(eb - e0) * NBLK * BS;
+    if ((reinterpret_cast<uintptr_t>(dst) & 15u) == 0 && (nfl & 3) == 0) {
+      const float4 *s4 = reinterpret_cast<const float4 *>(src);
+      float4 *d4 = reinterpret_cast<float4 *>(dst);
+      for (int64_t i = tid; i < nfl / 4; i += nth) d4[i] = s4[i];
+    } else {
+      for (int64_t i = tid; i < nfl; i += nth) dst[i] = src[i];
+    }
+  }
 }
 
 // ---- the element-block kernel of the single-matrix mixed path ---------------
@@ -392,7 +427,7 @@ inline int default_general_tile(int etype, int npts) {
 inline size_t tile_smem_bytes(int etype, int form, int npts, int te) {
   const int nne = nodes_per_elem(etype);
   if (form == F_DIFF_ISO || form == F_ELAST_ISO || form == F_DOT)
-    return fast_layout(nne, npts, te).total;
+    return fast_layout(nne, npts, te, 3).total;  // the largest block size (ndn 3)
   return mixed_layout(nne, manif_dim(etype), npts, te).total;
 }
 
@@ -416,6 +451,8 @@ __global__ void __launch_bounds__(kMixedThreads) k_blocks_mixed(const KArgs a) {
 
 template <int ET, int FORM, int NDN>
 int launch_blocks_mixed_t(const KArgs &a, int num_sms, cudaStream_t s) {
+  if constexpr (kFastForm<FORM>)
+    FEGPU_REQUIRE(a.te >= 1 && a.te <= max_fast_tile(ET), "mixed: elements per tile out of range");
   const size_t smem = tile_smem_bytes(ET, FORM, a.npts, a.te);
   auto kern = k_blocks_mixed<ET, FORM, NDN>;
   FEGPU_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
