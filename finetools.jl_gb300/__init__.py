@@ -11,10 +11,14 @@ package is the host-side mirror of the reference's Julia interface.
 from ._native import FegpuError, load as load_library
 from .batch import AssemblyBatch
 from .serve import AssemblyServer
-from .assembly import (DeviceMatrix, SysmatAssemblerGPU, SysvecAssemblerGPU, assemble,
-                       conjugategradient, makematrix, startassembly)
+from .assembly import (DeviceMatrix, SysmatAssemblerGPU, SysmatAssemblerSparseDiagGPU,
+                       SysmatAssemblerFFBlockGPU, SysmatAssemblerSparseHRZLumpingSymmGPU,
+                       SysvecAssemblerGPU, assemble,
+                       conjugategradient, makematrix, matrix_blocked_dd, matrix_blocked_df,
+                       matrix_blocked_fd, matrix_blocked_ff, startassembly)
 from .femm import (DataCache, DeforModelRed3D, ElementwiseData, FEMMBase, ForceIntensity,
-                   IntegDomain, IsotropicElementwise, bilform_diffusion, bilform_dot,
+                   IntegDomain, IsotropicElementwise, bilform_convection, bilform_diffusion, bilform_div_grad,
+                   bilform_dot, bilform_masslike,
                    bilform_lin_elastic, connectionmatrix, distribloads, innerproduct,
                    linform_dot)
 from .fesets import FESetH8, FESetH20, FESetQ4, FESetT4, FESetT10

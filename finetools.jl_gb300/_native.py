@@ -18,6 +18,7 @@ COEF_CONST, COEF_PER_ELEMENT, COEF_PER_QP, COEF_ISO_LAME = 0, 1, 2, 3
 FP64, MIXED = 0, 1
 FORM_DIFFUSION, FORM_LIN_ELASTIC, FORM_DOT = 0, 1, 2
 REQUEST_COEF, REQUEST_COORDS = 0, 1
+ASM_SPARSE, ASM_SPARSE_SYMM, ASM_SPARSE_DIAG, ASM_HRZ_LUMPING_SYMM = 0, 1, 2, 3
 
 EXPORTS = [
     "fegpu_last_error", "fegpu_context_create", "fegpu_context_destroy",
@@ -26,10 +27,11 @@ EXPORTS = [
     "fegpu_femm_set_geometry", "fegpu_femm_colors", "fegpu_dofmap_create",
     "fegpu_dofmap_destroy", "fegpu_dofmap_copy_pattern", "fegpu_matrix_create",
     "fegpu_matrix_destroy", "fegpu_bilform_diffusion", "fegpu_bilform_lin_elastic",
-    "fegpu_bilform_dot", "fegpu_linform_dot", "fegpu_matrix_nnz", "fegpu_matrix_copy_csc",
-    "fegpu_matrix_copy_values", "fegpu_matrix_spmv", "fegpu_matrix_cg", "fegpu_assembler_create",
+    "fegpu_bilform_dot", "fegpu_bilform_div_grad", "fegpu_bilform_convection", "fegpu_linform_dot", "fegpu_bilform_dot_lumped", "fegpu_matrix_nnz", "fegpu_matrix_copy_csc",
+    "fegpu_matrix_copy_values", "fegpu_matrix_copy_values_async", "fegpu_matrix_wait_export", "fegpu_matrix_copy_block_csc", "fegpu_matrix_spmv",
+    "fegpu_matrix_cg", "fegpu_assembler_create",
     "fegpu_assembler_destroy", "fegpu_assembler_assemble", "fegpu_assembler_make",
-    "fegpu_assembler_copy_csc", "fegpu_bilform_lin_elastic_noalloc",
+    "fegpu_assembler_copy_csc", "fegpu_bilform_masslike", "fegpu_bilform_lin_elastic_noalloc",
     "fegpu_batch_create", "fegpu_batch_destroy", "fegpu_batch_add", "fegpu_batch_set_coef",
     "fegpu_batch_tune", "fegpu_batch_tile", "fegpu_batch_set_wait_limit", "fegpu_batch_launch",
     "fegpu_batch_wait", "fegpu_batch_run", "fegpu_batch_stats",
@@ -81,11 +83,17 @@ def load(path: str = LIBPATH):
         "fegpu_matrix_destroy": ([vp], i32),
         "fegpu_bilform_diffusion": ([vp, C.POINTER(Coef), i32], i32),
         "fegpu_bilform_lin_elastic": ([vp, C.POINTER(Coef), i32], i32),
+        "fegpu_bilform_div_grad": ([vp, C.POINTER(Coef), i32], i32),
+        "fegpu_bilform_convection": ([vp, i32, vp], i32),
         "fegpu_bilform_dot": ([vp, C.POINTER(Coef), i32, i32, i32], i32),
         "fegpu_linform_dot": ([vp, C.POINTER(Coef), i32, vp], i32),
+        "fegpu_bilform_dot_lumped": ([vp, C.POINTER(Coef), i32, i32, vp], i32),
         "fegpu_matrix_nnz": ([vp, i32, p64], i32),
         "fegpu_matrix_copy_csc": ([vp, i32, vp, vp, vp], i32),
         "fegpu_matrix_copy_values": ([vp, vp], i32),
+        "fegpu_matrix_copy_values_async": ([vp, vp], i32),
+        "fegpu_matrix_wait_export": ([vp], i32),
+        "fegpu_matrix_copy_block_csc": ([vp, i64, i64, i64, i64, i32, p64, vp, vp, vp], i32),
         "fegpu_matrix_spmv": ([vp, vp, vp], i32),
         "fegpu_matrix_cg": ([vp, vp, vp, i32, vp], i32),
         "fegpu_assembler_create": ([vp, i32, i64, i64, pp], i32),
@@ -93,6 +101,7 @@ def load(path: str = LIBPATH):
         "fegpu_assembler_assemble": ([vp, vp, i32, i32, vp, vp], i32),
         "fegpu_assembler_make": ([vp, p64], i32),
         "fegpu_assembler_copy_csc": ([vp, vp, vp, vp], i32),
+        "fegpu_bilform_masslike": ([vp, C.POINTER(Coef), i32, vp, vp], i32),
         "fegpu_bilform_lin_elastic_noalloc": ([vp, C.POINTER(Coef)], i32),
         "fegpu_batch_create": ([vp, pp], i32),
         "fegpu_batch_destroy": ([vp], i32),

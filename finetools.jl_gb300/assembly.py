@@ -21,7 +21,7 @@ from . import _native as nat
 
 
 def _is_assembler(x) -> bool:
-    return isinstance(x, (SysmatAssemblerGPU, SysvecAssemblerGPU))
+    return isinstance(x, (SysmatAssemblerGPU, SysmatAssemblerFFBlockGPU, SysvecAssemblerGPU))
 
 
 class DeviceMatrix:
@@ -45,6 +45,23 @@ class DeviceMatrix:
 
     def __matmul__(self, x):
         return self.spmv(x)
+
+    def block(self, rows, cols, drop_zeros=None):
+        """CSC (scipy) of the block rows x cols (0-based ranges) of the matrix;
+        exact zeros left out as the assembler's result does (drop_zeros)."""
+        dz = int(self.drop_zeros if drop_zeros is None else drop_zeros)
+        r0, r1 = rows
+        c0, c1 = cols
+        L = nat.load()
+        nnz = C.c_int64()
+        nat.check(L.fegpu_matrix_copy_block_csc(self.h, r0, r1, c0, c1, dz, C.byref(nnz), None,
+                                                None, None))
+        colptr = np.empty(c1 - c0 + 1, dtype=np.int64)
+        rowval = np.empty(nnz.value, dtype=np.int64)
+        nzval = np.empty(nnz.value)
+        nat.check(L.fegpu_matrix_copy_block_csc(self.h, r0, r1, c0, c1, dz, C.byref(nnz),
+                                                nat.ptr(colptr), nat.ptr(rowval), nat.ptr(nzval)))
+        return sp.csc_matrix((nzval, rowval - 1, colptr - 1), shape=(r1 - r0, c1 - c0))
 
     def cg(self, b, x0, maxiter):
         """conjugategradient(K, b, x0, maxiter) on the device."""
@@ -80,13 +97,19 @@ class SysmatAssemblerGPU:
     symmetric=True reproduces SysmatAssemblerSparseSymm (the default of the
     symmetric forms: exact zeros of S + S' are not stored), symmetric=False
     SysmatAssemblerSparse (structural pattern kept).  precision "fp64" or
-    "mixed" (FP32 element arithmetic, FP64 global accumulation).
+    "mixed" (FP32 element arithmetic, FP64 global accumulation).  lumping
+    "diag" / "hrz" reproduces SysmatAssemblerSparseDiag /
+    SysmatAssemblerSparseHRZLumpingSymm (diagonal results; bilform_dot and the
+    generic protocol).
     """
 
     def __init__(self, symmetric: bool = True, precision: str = "fp64", result: str = "host",
-                 drop_zeros=None, device: int = 0):
+                 drop_zeros=None, device: int = 0, lumping=None):
         if precision not in ("fp64", "mixed"):
             raise ValueError("precision must be 'fp64' or 'mixed'")
+        if lumping not in (None, "diag", "hrz"):
+            raise ValueError("lumping must be None, 'diag' or 'hrz'")
+        self.lumping = lumping
         if result not in ("host", "device"):
             raise ValueError("result must be 'host' or 'device'")
         self.symmetric = symmetric
@@ -96,10 +119,18 @@ class SysmatAssemblerGPU:
         self.drop_zeros = symmetric if drop_zeros is None else bool(drop_zeros)
         self.device = device
         self._generic = None
+        self._generic_kind = None
+        self._generic_fin = None
+        self._shape = None
         self._nomatrixresult = False
 
     def eltype(self):
         return np.float64
+
+    def _post(self, A):
+        """The result handed to the caller (the wrapping FF-block assembler
+        cuts its block out)."""
+        return A
 
     # ---- device forms --------------------------------------------------------
     def _matrix_for(self, dm):
@@ -124,15 +155,34 @@ class SysmatAssemblerGPU:
         if self.symmetric and elem_mat_nrows != elem_mat_ncols:
             raise ValueError("Symmetric sparse matrix is assumed to be assembled from square "
                              "matrices")
-        if self._generic is None:
-            out = C.c_void_p()
-            nat.check(nat.load().fegpu_assembler_create(nat.context(self.device),
-                                                        int(self.symmetric), row_nalldofs,
-                                                        col_nalldofs, C.byref(out)))
-            self._generic = out.value
-            self._shape = (row_nalldofs, col_nalldofs)
-            weakref.finalize(self, nat.load().fegpu_assembler_destroy, self._generic)
+        kind = {None: nat.ASM_SPARSE_SYMM if self.symmetric else nat.ASM_SPARSE,
+                "diag": nat.ASM_SPARSE_DIAG, "hrz": nat.ASM_HRZ_LUMPING_SYMM}[self.lumping]
+        self._open_generic(kind, row_nalldofs, col_nalldofs)
         return self
+
+    def _open_generic(self, kind, nrows, ncols):
+        """A fresh device COO assembler of this kind and size: startassembly!
+        restarts the buffers, dropping triples assembled before."""
+        if self._generic_fin is not None:
+            self._generic_fin()
+        out = C.c_void_p()
+        nat.check(nat.load().fegpu_assembler_create(nat.context(self.device), kind,
+                                                    int(nrows), int(ncols), C.byref(out)))
+        self._generic = out.value
+        self._generic_kind = kind
+        self._shape = (int(nrows), int(ncols))
+        self._generic_fin = weakref.finalize(self, nat.load().fegpu_assembler_destroy,
+                                             self._generic)
+        return self._generic
+
+    def _generic_csc(self, nnz):
+        """Copy the made matrix of the device COO assembler out as scipy CSC."""
+        colptr = np.empty(self._shape[1] + 1, dtype=np.int64)
+        rowval = np.empty(nnz, dtype=np.int64)
+        nzval = np.empty(nnz)
+        nat.check(nat.load().fegpu_assembler_copy_csc(self._generic, nat.ptr(colptr),
+                                                      nat.ptr(rowval), nat.ptr(nzval)))
+        return sp.csc_matrix((nzval, rowval - 1, colptr - 1), shape=self._shape)
 
     def assemble(self, mat, dofnums_row, dofnums_col):
         if self._generic is None:
@@ -151,12 +201,64 @@ class SysmatAssemblerGPU:
             return sp.csc_matrix(self._shape)
         nnz = C.c_int64()
         nat.check(nat.load().fegpu_assembler_make(self._generic, C.byref(nnz)))
-        colptr = np.empty(self._shape[1] + 1, dtype=np.int64)
-        rowval = np.empty(nnz.value, dtype=np.int64)
-        nzval = np.empty(nnz.value)
-        nat.check(nat.load().fegpu_assembler_copy_csc(self._generic, nat.ptr(colptr),
-                                                      nat.ptr(rowval), nat.ptr(nzval)))
-        return sp.csc_matrix((nzval, rowval - 1, colptr - 1), shape=self._shape)
+        return self._generic_csc(nnz.value)
+
+
+class SysmatAssemblerFFBlockGPU:
+    """SysmatAssemblerFFBlock (src/AssemblyModule.jl:1144-1236): the assembly
+    is delegated to a wrapped GPU assembler (by default
+    SysmatAssemblerGPU(symmetric=False), the reference's
+    SysmatAssemblerSparse) and the result is its free-free block
+    (matrix_blocked_ff: rows 1..row_nfreedofs, columns 1..col_nfreedofs),
+    cut out on the device for the device forms.  The result is a scipy CSC
+    matrix."""
+
+    def __init__(self, row_nfreedofs, col_nfreedofs=None, a=None, device: int = 0):
+        if isinstance(row_nfreedofs, SysmatAssemblerGPU):
+            # SysmatAssemblerFFBlock(a, row_nfreedofs, col_nfreedofs)
+            a, row_nfreedofs, col_nfreedofs = row_nfreedofs, col_nfreedofs, a
+        self._a = a if a is not None else SysmatAssemblerGPU(symmetric=False, device=device)
+        self._row_nfreedofs = int(row_nfreedofs)
+        self._col_nfreedofs = int(row_nfreedofs if col_nfreedofs is None else col_nfreedofs)
+
+    # the wrapped assembler's settings
+    symmetric = property(lambda self: self._a.symmetric)
+    precision = property(lambda self: self._a.precision)
+    precision_code = property(lambda self: self._a.precision_code)
+    lumping = property(lambda self: self._a.lumping)
+    drop_zeros = property(lambda self: self._a.drop_zeros)
+
+    def eltype(self):
+        return self._a.eltype()
+
+    def _post(self, A):
+        return _blocked(A, "ff", self._row_nfreedofs, self._col_nfreedofs)
+
+    def _run(self, dm, call):
+        h = self._a._matrix_for(dm)
+        nat.check(call(h))
+        return self._post(DeviceMatrix(h, dm, self._a.drop_zeros))
+
+    def startassembly(self, *args, **kw):
+        self._a.startassembly(*args, **kw)
+        return self
+
+    def assemble(self, mat, dofnums_row, dofnums_col):
+        self._a.assemble(mat, dofnums_row, dofnums_col)
+        return self
+
+    def makematrix(self):
+        return self._post(self._a.makematrix())
+
+
+def SysmatAssemblerSparseDiagGPU(device: int = 0):
+    """SysmatAssemblerSparseDiag on the GPU (src/AssemblyModule.jl:599-794)."""
+    return SysmatAssemblerGPU(symmetric=True, lumping="diag", device=device)
+
+
+def SysmatAssemblerSparseHRZLumpingSymmGPU(device: int = 0):
+    """SysmatAssemblerSparseHRZLumpingSymm on the GPU (src/AssemblyModule.jl:943-1145)."""
+    return SysmatAssemblerGPU(symmetric=True, lumping="hrz", device=device)
 
 
 class SysvecAssemblerGPU:
@@ -169,6 +271,45 @@ class SysvecAssemblerGPU:
         F = np.zeros(dm.ndof)
         nat.check(nat.load().fegpu_linform_dot(dm.h, C.byref(coef), m, nat.ptr(F)))
         return F
+
+
+def _blocked(A, which, row_nfreedofs, col_nfreedofs):
+    """One of the four blocks of A: on the device for a DeviceMatrix, else
+    by slicing the (scipy) matrix as the reference slices its
+    SparseMatrixCSC (stored entries kept)."""
+    col_nfreedofs = row_nfreedofs if col_nfreedofs is None else col_nfreedofs
+    n, m = A.shape
+    if row_nfreedofs > n:
+        raise ValueError("The ff block has too many rows")
+    if col_nfreedofs > m:
+        raise ValueError("The ff block has too many columns")
+    rows = (0, row_nfreedofs) if which[0] == "f" else (row_nfreedofs, n)
+    cols = (0, col_nfreedofs) if which[1] == "f" else (col_nfreedofs, m)
+    if isinstance(A, DeviceMatrix):
+        return A.block(rows, cols)
+    if not sp.issparse(A):
+        raise TypeError("blocked extraction takes a DeviceMatrix or a scipy sparse matrix")
+    return sp.csc_matrix(A)[rows[0]:rows[1], cols[0]:cols[1]]
+
+
+def matrix_blocked_ff(A, row_nfreedofs, col_nfreedofs=None):
+    """matrix_blocked_ff (src/MatrixUtilityModule.jl:675-688): the free-free block."""
+    return _blocked(A, "ff", row_nfreedofs, col_nfreedofs)
+
+
+def matrix_blocked_fd(A, row_nfreedofs, col_nfreedofs=None):
+    """matrix_blocked_fd (src/MatrixUtilityModule.jl:708-723)."""
+    return _blocked(A, "fd", row_nfreedofs, col_nfreedofs)
+
+
+def matrix_blocked_df(A, row_nfreedofs, col_nfreedofs=None):
+    """matrix_blocked_df (src/MatrixUtilityModule.jl:743-758)."""
+    return _blocked(A, "df", row_nfreedofs, col_nfreedofs)
+
+
+def matrix_blocked_dd(A, row_nfreedofs, col_nfreedofs=None):
+    """matrix_blocked_dd (src/MatrixUtilityModule.jl:778-793)."""
+    return _blocked(A, "dd", row_nfreedofs, col_nfreedofs)
 
 
 def conjugategradient(A, b, x0, maxiter):

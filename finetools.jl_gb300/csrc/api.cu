@@ -73,7 +73,10 @@ int choose_tile(int etype, int form, int precision, int npts) {
   const int nne = nodes_per_elem(etype), mdim = manif_dim(etype);
   const bool grad = form <= F_ELAST_GEN;
   const int tsize = (precision == FEGPU_MIXED && grad) ? 4 : 8;
-  const size_t budget = (etype == FEGPU_H20) ? 200 * 1024 : 100 * 1024;
+  // shared-memory budget per CTA: measured on T10 60^3 elasticity (FP64),
+  // 72 KB (32 elements per tile) runs 1.36x faster than 100 KB (44): finer
+  // tiles balance the pair-block rounds and the waves of a colour better
+  const size_t budget = (etype == FEGPU_H20) ? 200 * 1024 : 72 * 1024;
   const SmemLayout one = smem_layout(nne, mdim, npts, 1, tsize, grad);
   const SmemLayout two = smem_layout(nne, mdim, npts, 2, tsize, grad);
   const size_t per = two.total - one.total;
@@ -198,8 +201,13 @@ void pack_geometry(const double *src_colmajor, int64_t nnodes, int sdim, double 
   FEGPU_CUDA(cudaGetLastError());
 }
 
+void await_export(fegpu_matrix *K, cudaStream_t s) {
+  if (K && K->export_pending) FEGPU_CUDA(cudaStreamWaitEvent(s, K->exported, 0));
+}
+
 KArgs base_args(fegpu_matrix *K, fegpu_dofmap *dm) {
   fegpu_femm *fm = dm->femm;
+  await_export(K, fm->ctx->stream);
   KArgs a;
   std::memset(&a, 0, sizeof(a));
   a.conn = fm->conn.as<int32_t>();
@@ -230,11 +238,19 @@ void run_colours(fegpu_dofmap *dm, int form, int precision, KArgs &a) {
   fegpu_context *ctx = fm->ctx;
   const int ncol = static_cast<int>(fm->color_offsets.size()) - 1;
   if (ctx->timing) FEGPU_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
+  const int te_max = a.te;
+  const bool fixed = std::getenv("FEGPU_FP64_TILE") != nullptr;
   for (int c = 0; c < ncol; ++c) {
     a.e0 = fm->color_offsets[c];
     a.e1 = fm->color_offsets[c + 1];
+    // small colours: smaller tiles, so that every SM gets about two CTAs
+    // (H8 20^3 diffusion, 1,000-element colours: 0.24 ms at 12 per tile
+    // against 0.35 ms at 21)
+    const int64_t per = (a.e1 - a.e0 + 2 * ctx->num_sms - 1) / (2 * ctx->num_sms);
+    a.te = fixed ? te_max : static_cast<int>(std::max<int64_t>(4, std::min<int64_t>(te_max, per)));
     ctx->launches += launch_form(fm->etype, form, precision, dm->ndn, a, ctx->num_sms, ctx->stream);
   }
+  a.te = te_max;
   if (ctx->timing) {
     FEGPU_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
     FEGPU_CUDA(cudaEventSynchronize(ctx->ev1));
@@ -287,6 +303,14 @@ void run_gather(fegpu_dofmap *dm, int form, KArgs &a) {
     ctx->ev_blocks.push_back(e1);
     ctx->ev_gather.push_back(e2);
   }
+  // the element-block grid covers a share of the SMs' CTA slots, so the
+  // gathers find room beside it (FEGPU_MIXED_BLOCK_SHARE overrides, 0..1)
+  double share = 1.0;
+  if (const char *env = std::getenv("FEGPU_MIXED_BLOCK_SHARE")) {
+    const double v = std::atof(env);
+    if (v > 0.0 && v <= 1.0) share = v;
+  }
+  const int block_sms = std::max(1, static_cast<int>(ctx->num_sms * share));
   if (ctx->timing) FEGPU_CUDA(cudaEventRecord(ctx->ev0, s0));
   FEGPU_CUDA(cudaEventRecord(ctx->ev_gather[0], s0));  // work before this call
   FEGPU_CUDA(cudaStreamWaitEvent(ctx->side, ctx->ev_gather[0], 0));
@@ -299,7 +323,7 @@ void run_gather(fegpu_dofmap *dm, int form, KArgs &a) {
     a.e0 = c * dm->chunk;
     a.e1 = std::min(fm->nelem, (c + 1) * dm->chunk);
     a.ke = dm->ke.as<float>() + slot * dm->chunk * nblk * bs;
-    ctx->launches += launch_mixed(fm->etype, form, a, ctx->num_sms, ctx->side);
+    ctx->launches += launch_mixed(fm->etype, form, a, block_sms, ctx->side);
     FEGPU_CUDA(cudaEventRecord(ctx->ev_blocks[slot], ctx->side));
     FEGPU_CUDA(cudaStreamWaitEvent(s0, ctx->ev_blocks[slot], 0));
     g.n0 = dm->chunk_nodes[c];
@@ -415,6 +439,10 @@ int fegpu_context_destroy(fegpu_context *ctx) {
     for (cudaEvent_t e : ctx->ev_blocks) cudaEventDestroy(e);
     for (cudaEvent_t e : ctx->ev_gather) cudaEventDestroy(e);
     if (ctx->side) cudaStreamDestroy(ctx->side);
+    if (ctx->export_stream) {
+      cudaStreamSynchronize(ctx->export_stream);
+      cudaStreamDestroy(ctx->export_stream);
+    }
     ctx->scratch.release();
     ctx->scratch2.release();
     cudaStreamDestroy(ctx->stream);
@@ -621,6 +649,9 @@ int fegpu_matrix_destroy(fegpu_matrix *K) {
     if (!K) return;
     cudaSetDevice(K->dm->femm->ctx->device);
     cudaStreamSynchronize(K->dm->femm->ctx->stream);
+    if (K->exported) cudaEventSynchronize(K->exported);  // a copy may still read val
+    if (K->ready) cudaEventDestroy(K->ready);
+    if (K->exported) cudaEventDestroy(K->exported);
     delete K;
   });
 }
@@ -650,6 +681,7 @@ int fegpu_bilform_diffusion(fegpu_matrix *K, const fegpu_coef *cf, int precision
                     "diffusion: a matrix coefficient must be constant or per element");
       form = F_DIFF_GEN;
     }
+    K->unsym = false;
     KArgs a = base_args(K, dm);
     CoefStage st;
     const bool gather = precision == FEGPU_MIXED;
@@ -670,6 +702,7 @@ int fegpu_bilform_lin_elastic(fegpu_matrix *K, const fegpu_coef *cf, int precisi
     FEGPU_REQUIRE(fm->mdim == 3 && fm->sdim == 3, "lin_elastic: 3-D solid elements only");
     FEGPU_REQUIRE(dm->ndn == 3, "lin_elastic: the field must have three DOFs per node");
     FEGPU_REQUIRE(precision == FEGPU_FP64 || precision == FEGPU_MIXED, "unknown precision");
+    K->unsym = false;
     KArgs a = base_args(K, dm);
     CoefStage st;
     int form;
@@ -703,6 +736,48 @@ int fegpu_bilform_lin_elastic(fegpu_matrix *K, const fegpu_coef *cf, int precisi
   });
 }
 
+// bilform_div_grad (src/FEMMBaseModule.jl:1672-1723): block (a, b) of the
+// element matrix is mu (g_a . g_b I + g_b g_a^T) summed over the points, i.e.
+// the isotropic elasticity block with lambda = 0 and mu = the viscosity; the
+// element kernels of bilform_lin_elastic evaluate it.
+int fegpu_bilform_div_grad(fegpu_matrix *K, const fegpu_coef *cf, int precision) {
+  return guarded([&] {
+    FEGPU_REQUIRE(K && cf && cf->data, "null handle");
+    fegpu_dofmap *dm = K->dm;
+    fegpu_femm *fm = dm->femm;
+    use_device(fm->ctx);
+    require_geometry(fm);
+    FEGPU_REQUIRE(fm->mdim == 3 && fm->sdim == 3 && dm->ndn == 3,
+                  "div_grad: 3-D elements with a three-component field");
+    FEGPU_REQUIRE(precision == FEGPU_FP64 || precision == FEGPU_MIXED, "unknown precision");
+    FEGPU_REQUIRE(cf->ncomp == 1, "div_grad: the viscosity must be a scalar");
+    K->unsym = false;
+    KArgs a = base_args(K, dm);
+    CoefStage st;
+    const bool gather = precision == FEGPU_MIXED;
+    if (cf->kind == FEGPU_COEF_CONST) {
+      a.coef_kind = FEGPU_COEF_CONST;
+      a.ncomp = 2;
+      a.cconst[0] = 0.0;
+      a.cconst[1] = cf->data[0];
+    } else if (cf->kind == FEGPU_COEF_PER_ELEMENT) {
+      std::vector<double> lame(static_cast<size_t>(2 * fm->nelem));
+      for (int64_t e = 0; e < fm->nelem; ++e) {
+        lame[2 * e] = 0.0;
+        lame[2 * e + 1] = cf->data[e];
+      }
+      const fegpu_coef pairs{FEGPU_COEF_ISO_LAME, 2, lame.data()};
+      stage_coef(fm, &pairs, 2, a, st, !gather);
+      FEGPU_CUDA(cudaStreamSynchronize(fm->ctx->stream));  // lame leaves scope
+    } else {
+      throw Error{FEGPU_ERR_ARG, "div_grad: viscosity constant or per element"};
+    }
+    if (!gather) zero_matrix(K);
+    if (fm->nelem > 0) run_form(dm, F_ELAST_ISO, precision, a);
+    FEGPU_CUDA(cudaStreamSynchronize(fm->ctx->stream));
+  });
+}
+
 int fegpu_bilform_dot(fegpu_matrix *K, const fegpu_coef *cf, int m, int symmetric, int precision) {
   return guarded([&] {
     FEGPU_REQUIRE(K && cf, "null handle");
@@ -730,6 +805,11 @@ int fegpu_bilform_dot(fegpu_matrix *K, const fegpu_coef *cf, int m, int symmetri
       for (int i = 0; i < ndn * ndn; ++i) c[i] = cf->data[i];
       a.coef_kind = FEGPU_COEF_CONST;
     }
+    K->unsym = false;
+    if (!symmetric)
+      for (int i = 0; i < ndn; ++i)
+        for (int j = 0; j < ndn; ++j)
+          if (c[i * ndn + j] != c[j * ndn + i]) K->unsym = true;
     // element-matrix entry (k,p),(l,q) is N_k N_l c[p][q] (src/FEMMBaseModule.jl:1357-1361);
     // the symmetric assembler keeps its lower triangle by local index and mirrors it.
     for (int i = 0; i < ndn; ++i)
@@ -788,7 +868,39 @@ int fegpu_matrix_copy_csc(fegpu_matrix *K, int drop_zeros, int64_t *colptr, int6
   return guarded([&] {
     FEGPU_REQUIRE(K && colptr && rowval && nzval, "null handle");
     use_device(K->dm->femm->ctx);
-    copy_csc(K->dm->femm->ctx, K->dm, K->val.as<double>(), drop_zeros, colptr, rowval, nzval);
+    if (K->unsym) {  // CSC of an unsymmetric matrix: the values read by columns
+      DevBuf t;
+      t.alloc(sizeof(double) * std::max<int64_t>(K->dm->nnz, 1));
+      transpose_values(K->dm, K->val.as<double>(), t.as<double>(), K->dm->femm->ctx->stream);
+      copy_csc(K->dm->femm->ctx, K->dm, t.as<double>(), drop_zeros, colptr, rowval, nzval);
+    } else {
+      copy_csc(K->dm->femm->ctx, K->dm, K->val.as<double>(), drop_zeros, colptr, rowval, nzval);
+    }
+  });
+}
+
+int fegpu_matrix_copy_block_csc(fegpu_matrix *K, int64_t row0, int64_t row1, int64_t col0,
+                                int64_t col1, int drop_zeros, int64_t *nnz, int64_t *colptr,
+                                int64_t *rowval, double *nzval) {
+  return guarded([&] {
+    FEGPU_REQUIRE(K && nnz, "null handle");
+    const fegpu_dofmap *dm = K->dm;
+    FEGPU_REQUIRE(0 <= row0 && row0 <= row1 && row1 <= dm->ndof, "The ff block has too many rows");
+    FEGPU_REQUIRE(0 <= col0 && col0 <= col1 && col1 <= dm->ndof,
+                  "The ff block has too many columns");
+    FEGPU_REQUIRE((colptr == nullptr) == (rowval == nullptr) && (rowval == nullptr) == (nzval == nullptr),
+                  "colptr, rowval and nzval: all or none");
+    fegpu_context *ctx = dm->femm->ctx;
+    use_device(ctx);
+    DevBuf t;
+    const double *v = K->val.as<double>();
+    if (K->unsym) {
+      t.alloc(sizeof(double) * std::max<int64_t>(dm->nnz, 1));
+      transpose_values(dm, K->val.as<double>(), t.as<double>(), ctx->stream);
+      v = t.as<double>();
+    }
+    *nnz = copy_block_csc(ctx, dm, v, row0, row1, col0, col1, drop_zeros, colptr, rowval,
+                          nzval);
   });
 }
 
@@ -800,6 +912,32 @@ int fegpu_matrix_copy_values(fegpu_matrix *K, double *nzval) {
     FEGPU_CUDA(cudaMemcpyAsync(nzval, K->val.p, sizeof(double) * K->dm->nnz,
                                cudaMemcpyDeviceToHost, ctx->stream));
     FEGPU_CUDA(cudaStreamSynchronize(ctx->stream));
+  });
+}
+
+int fegpu_matrix_copy_values_async(fegpu_matrix *K, double *nzval) {
+  return guarded([&] {
+    FEGPU_REQUIRE(K && nzval, "null handle");
+    fegpu_context *ctx = K->dm->femm->ctx;
+    use_device(ctx);
+    if (!ctx->export_stream)
+      FEGPU_CUDA(cudaStreamCreateWithFlags(&ctx->export_stream, cudaStreamNonBlocking));
+    if (!K->ready) FEGPU_CUDA(cudaEventCreateWithFlags(&K->ready, cudaEventDisableTiming));
+    if (!K->exported) FEGPU_CUDA(cudaEventCreateWithFlags(&K->exported, cudaEventDisableTiming));
+    FEGPU_CUDA(cudaEventRecord(K->ready, ctx->stream));
+    FEGPU_CUDA(cudaStreamWaitEvent(ctx->export_stream, K->ready, 0));
+    FEGPU_CUDA(cudaMemcpyAsync(nzval, K->val.p, sizeof(double) * K->dm->nnz,
+                               cudaMemcpyDeviceToHost, ctx->export_stream));
+    FEGPU_CUDA(cudaEventRecord(K->exported, ctx->export_stream));
+    K->export_pending = true;
+  });
+}
+
+int fegpu_matrix_wait_export(fegpu_matrix *K) {
+  return guarded([&] {
+    FEGPU_REQUIRE(K, "null handle");
+    use_device(K->dm->femm->ctx);
+    if (K->export_pending) FEGPU_CUDA(cudaEventSynchronize(K->exported));
   });
 }
 

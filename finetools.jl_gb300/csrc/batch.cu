@@ -263,6 +263,7 @@ void make_batch_job(fegpu_matrix *K, int form, int code, int m, const fegpu_coef
   const int nne = fm->nne, ndn = dm->ndn;
   const int64_t elem_floats = static_cast<int64_t>(nne) * (nne + 1) / 2 * ndn * ndn;
   if (!dm->gather_ready) build_gather_plan(dm, static_cast<int>(elem_floats));
+  K->unsym = false;
   KArgs a = base_args(K, dm);
   a.conn = fm->conn_orig.as<int32_t>();
   a.measure_m = m;
@@ -555,6 +556,7 @@ int fegpu_batch_launch(fegpu_batch *b) {
       FEGPU_CUDA(cudaGraphInstantiate(&b->exec, b->graph, 0));
     }
     fegpu_context *ctx = b->ctx;
+    for (const auto &J : b->jobs) await_export(J.K, st);  // outside the captured graph
     if (ctx->timing) FEGPU_CUDA(cudaEventRecord(ctx->ev0, st));
     FEGPU_CUDA(cudaGraphLaunch(b->exec, st));
     if (ctx->timing) FEGPU_CUDA(cudaEventRecord(ctx->ev1, st));

@@ -517,31 +517,43 @@ __global__ void __launch_bounds__(kFormThreads) k_form(const KArgs a) {
         }
       }
 
-      // ---- scatter (no atomics: one colour's elements share no node)
+      // ---- scatter (no atomics: one colour's elements share no node).  The
+      // block's slots are distinct, so all row offsets, then all current
+      // values are loaded before any store: independent loads in flight
+      // together instead of one read-modify-write round trip per entry.
       const int32_t A = sConn[e * NNE + pa], B = sConn[e * NNE + pb];
+      const bool off_diag = pa != pb;
       const int pAB = a.pos[(es * NNE + pa) * NNE + pb];
+      const int pBA = off_diag ? a.pos[(es * NNE + pb) * NNE + pa] : 0;
+      int64_t rA[NDN], rB[NDN], cA[NDN], cB[NDN];
 #pragma unroll
       for (int ii = 0; ii < NDN; ++ii) {
-        const int64_t r0 = a.rowptr[a.dof[A * NDN + ii]];
-#pragma unroll
-        for (int jj = 0; jj < NDN; ++jj) {
-          const int64_t off = a.colperm ? a.colperm[a.cpoff[A] * NDN + NDN * pAB + jj]
-                                        : static_cast<int64_t>(NDN * pAB + jj);
-          a.val[r0 + off] += double(V[ii][jj]);
-        }
+        rA[ii] = a.rowptr[a.dof[A * NDN + ii]];
+        rB[ii] = off_diag ? a.rowptr[a.dof[B * NDN + ii]] : 0;
+        cA[ii] = a.colperm ? a.colperm[a.cpoff[A] * NDN + NDN * pAB + ii]
+                           : static_cast<int64_t>(NDN * pAB + ii);
+        cB[ii] = !off_diag ? 0
+                 : a.colperm ? a.colperm[a.cpoff[B] * NDN + NDN * pBA + ii]
+                             : static_cast<int64_t>(NDN * pBA + ii);
       }
-      if (pa != pb) {
-        const int pBA = a.pos[(es * NNE + pb) * NNE + pa];
+      double cur[NDN][NDN], curt[NDN][NDN];
+#pragma unroll
+      for (int ii = 0; ii < NDN; ++ii)
 #pragma unroll
         for (int jj = 0; jj < NDN; ++jj) {
-          const int64_t r0 = a.rowptr[a.dof[B * NDN + jj]];
-#pragma unroll
-          for (int ii = 0; ii < NDN; ++ii) {
-            const int64_t off = a.colperm ? a.colperm[a.cpoff[B] * NDN + NDN * pBA + ii]
-                                          : static_cast<int64_t>(NDN * pBA + ii);
-            a.val[r0 + off] += double(Vt[jj][ii]);
-          }
+          cur[ii][jj] = a.val[rA[ii] + cA[jj]];
+          curt[jj][ii] = off_diag ? a.val[rB[jj] + cB[ii]] : 0.0;
         }
+#pragma unroll
+      for (int ii = 0; ii < NDN; ++ii)
+#pragma unroll
+        for (int jj = 0; jj < NDN; ++jj) a.val[rA[ii] + cA[jj]] = cur[ii][jj] + double(V[ii][jj]);
+      if (off_diag) {
+#pragma unroll
+        for (int jj = 0; jj < NDN; ++jj)
+#pragma unroll
+          for (int ii = 0; ii < NDN; ++ii)
+            a.val[rB[jj] + cB[ii]] = curt[jj][ii] + double(Vt[jj][ii]);
       }
     }
   }

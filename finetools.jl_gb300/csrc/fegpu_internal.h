@@ -95,6 +95,8 @@ struct fegpu_context {
   // overlap chunk c's gather; events per ring slot order them (created on use)
   cudaStream_t side = nullptr;
   std::vector<cudaEvent_t> ev_blocks, ev_gather;
+  // copies of finished matrices to host memory (fegpu_matrix_copy_values_async)
+  cudaStream_t export_stream = nullptr;
 };
 
 struct fegpu_femm {
@@ -151,7 +153,12 @@ struct fegpu_dofmap {
 
 struct fegpu_matrix {
   fegpu_dofmap *dm = nullptr;
-  fegpu::DevBuf val;  // double [nnz]
+  fegpu::DevBuf val;    // double [nnz], CSR order (row = test DOF)
+  bool unsym = false;   // values not symmetric: the CSC export transposes them
+  // asynchronous export: `ready` marks the values on the context stream,
+  // `exported` the end of their copy on the export stream
+  cudaEvent_t ready = nullptr, exported = nullptr;
+  bool export_pending = false;
 };
 
 namespace fegpu {
@@ -241,13 +248,48 @@ void pack_geometry(const double *src_colmajor, int64_t nnodes, int sdim, double 
 
 // ---- shared by the entry points -----------------------------------------------------
 KArgs base_args(fegpu_matrix *K, fegpu_dofmap *dm);
+// work queued on s after this call may overwrite K's values: it first waits
+// (on the device) for a copy of them still in flight to the host
+void await_export(fegpu_matrix *K, cudaStream_t s);
 bool is_isotropic(const double *D, double &lam, double &mu);
 
 // ---- matrix utilities -----------------------------------------------------------
 void spmv(const fegpu_dofmap *dm, const double *val, const double *x, double *y,
           cudaStream_t s);
 int64_t count_nonzeros(fegpu_context *ctx, const fegpu_dofmap *dm, const double *val);
+// CSR values -> the values of the same (symmetric) pattern read by columns:
+// out[slot of (j, i) in row j] = val[slot of (i, j) in row i]
+void transpose_values(const fegpu_dofmap *dm, const double *val, double *out, cudaStream_t s);
+// CSC (1-based) of the block rows [r0, r1) x columns [c0, c1) of a matrix of the
+// dofmap's pattern whose values are given by columns (exact zeros left out when
+// drop_zeros); colptr == nullptr: only returns the block's stored entries
+int64_t copy_block_csc(fegpu_context *ctx, const fegpu_dofmap *dm, const double *val, int64_t r0,
+                       int64_t r1, int64_t c0, int64_t c1, int drop_zeros, int64_t *colptr,
+                       int64_t *rowval, double *nzval);
 void copy_csc(fegpu_context *ctx, const fegpu_dofmap *dm, const double *val,
               int drop_zeros, int64_t *colptr, int64_t *rowval, double *nzval);
+}  // namespace fegpu
+
+// Generic COO assembler (matrix.cu): the triples of assemble! (host), or
+// keys and values formed on the device; makematrix! leaves the result as
+// sorted unique keys (column << 32 | row, 0-based) and values.
+struct fegpu_assembler {
+  fegpu_context *ctx = nullptr;
+  int symmetric = 0;  // S + S^T completion (SparseSymm)
+  int kind = 0;       // FEGPU_ASM_*
+  int64_t nrows = 0, ncols = 0;
+  std::vector<int64_t> I, J;
+  std::vector<double> V;
+  int64_t nnz = -1;
+  fegpu::DevBuf keys, vals;
+};
+
+namespace fegpu {
+// makematrix! on device COO data: key[t] = column << 32 | row (0-based),
+// idx[t] = t, V[t] the value of triple t in assembly order; the stable sort
+// sums duplicates in that order (sparse(I, J, V)), then the symmetric
+// completion if the assembler is SparseSymm.  Returns the stored entries.
+int64_t assembler_reduce(fegpu_assembler *a, DevBuf &key, DevBuf &idx, const double *V,
+                         int64_t n);
 
 }  // namespace fegpu

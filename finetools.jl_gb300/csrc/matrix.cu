@@ -118,6 +118,134 @@ int64_t count_nonzeros(fegpu_context *ctx, const fegpu_dofmap *dm, const double 
 }
 
 // CSC (== CSR of the symmetric matrix), 1-based.  val == nullptr: pattern only.
+namespace {
+// warp per row i: each entry (i, j) finds i in row j (sorted columns) and
+// writes its value there
+__global__ void k_transpose_vals(const int64_t *rowptr, const int32_t *colind, const double *val,
+                                 int64_t nrows, double *out) {
+  const int lane = threadIdx.x & 31;
+  const int64_t w0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t i = w0; i < nrows; i += nw) {
+    for (int64_t p = rowptr[i] + lane; p < rowptr[i + 1]; p += 32) {
+      const int32_t j = colind[p];
+      int64_t lo = rowptr[j], hi = rowptr[j + 1] - 1;
+      while (lo < hi) {
+        const int64_t mid = (lo + hi) >> 1;
+        if (colind[mid] < i) lo = mid + 1;
+        else hi = mid;
+      }
+      out[lo] = val[p];
+    }
+  }
+}
+}  // namespace
+
+namespace {
+__device__ __forceinline__ int64_t lower_bound32(const int32_t *a, int64_t lo, int64_t hi, int32_t v) {
+  while (lo < hi) {
+    const int64_t mid = (lo + hi) >> 1;
+    if (a[mid] < v) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// per column j in [c0, c1): the slice of its (sorted) row list in [r0, r1)
+// and the entries it keeps (all, or the nonzero ones when drop_zeros)
+__global__ void k_block_count(const int64_t *rowptr, const int32_t *colind, const double *val,
+                              int64_t c0, int64_t c1, int32_t r0, int32_t r1, int drop_zeros,
+                              int64_t *first, int64_t *last, int64_t *cnt) {
+  for (int64_t j = c0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < c1;
+       j += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t a = lower_bound32(colind, rowptr[j], rowptr[j + 1], r0);
+    const int64_t b = lower_bound32(colind, a, rowptr[j + 1], r1);
+    first[j - c0] = a;
+    last[j - c0] = b;
+    int64_t n = b - a;
+    if (drop_zeros) {
+      n = 0;
+      for (int64_t p = a; p < b; ++p) n += (val[p] != 0.0);
+    }
+    cnt[j - c0] = n;
+  }
+}
+
+// one warp per column; ballot compaction keeps the row order
+__global__ void k_block_copy(const int32_t *colind, const double *val, const int64_t *first,
+                             const int64_t *last, const int64_t *ptr, int64_t ncols, int32_t r0,
+                             int drop_zeros, int64_t *rowval, double *nzval) {
+  const int lane = threadIdx.x & 31;
+  const int64_t w0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t j = w0; j < ncols; j += nw) {
+    int64_t out = ptr[j];
+    for (int64_t p0 = first[j]; p0 < last[j]; p0 += 32) {
+      const int64_t p = p0 + lane;
+      const bool keep = p < last[j] && (!drop_zeros || val[p] != 0.0);
+      const unsigned m = __ballot_sync(0xffffffffu, keep);
+      if (keep) {
+        const int64_t o = out + __popc(m & ((1u << lane) - 1u));
+        rowval[o] = static_cast<int64_t>(colind[p]) - r0 + 1;
+        nzval[o] = val[p];
+      }
+      out += __popc(m);
+    }
+  }
+}
+}  // namespace
+
+int64_t copy_block_csc(fegpu_context *ctx, const fegpu_dofmap *dm, const double *val, int64_t r0,
+                       int64_t r1, int64_t c0, int64_t c1, int drop_zeros, int64_t *colptr,
+                       int64_t *rowval, double *nzval) {
+  cudaStream_t s = ctx->stream;
+  const int64_t nc = c1 - c0;
+  DevBuf first, last, cnt, ptr, tmp, rv, nz;
+  first.alloc(sizeof(int64_t) * (nc + 1));
+  last.alloc(sizeof(int64_t) * (nc + 1));
+  cnt.alloc(sizeof(int64_t) * (nc + 1));
+  ptr.alloc(sizeof(int64_t) * (nc + 1));
+  FEGPU_CUDA(cudaMemsetAsync(cnt.p, 0, sizeof(int64_t) * (nc + 1), s));
+  if (nc > 0) {
+    k_block_count<<<grid_of(nc), 256, 0, s>>>(dm->rowptr.as<int64_t>(), dm->colind.as<int32_t>(),
+                                              val, c0, c1, static_cast<int32_t>(r0),
+                                              static_cast<int32_t>(r1), drop_zeros,
+                                              first.as<int64_t>(), last.as<int64_t>(),
+                                              cnt.as<int64_t>());
+    FEGPU_CUDA(cudaGetLastError());
+  }
+  cub_call(ctx, tmp, [&](void *t, size_t &b) {
+    return cub::DeviceScan::ExclusiveSum(t, b, cnt.as<int64_t>(), ptr.as<int64_t>(), nc + 1, s);
+  });
+  int64_t nnz = 0;
+  FEGPU_CUDA(cudaMemcpyAsync(&nnz, ptr.as<int64_t>() + nc, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  FEGPU_CUDA(cudaStreamSynchronize(s));
+  if (!colptr) return nnz;  // size query
+  rv.alloc(sizeof(int64_t) * (nnz + 1));
+  nz.alloc(sizeof(double) * (nnz + 1));
+  if (nnz > 0)
+    k_block_copy<<<grid_of(nc * 32), 256, 0, s>>>(dm->colind.as<int32_t>(), val, first.as<int64_t>(),
+                                                  last.as<int64_t>(), ptr.as<int64_t>(), nc,
+                                                  static_cast<int32_t>(r0), drop_zeros,
+                                                  rv.as<int64_t>(), nz.as<double>());
+  FEGPU_CUDA(cudaGetLastError());
+  k_plus1<<<grid_of(nc + 1), 256, 0, s>>>(ptr.as<int64_t>(), nc + 1, first.as<int64_t>());
+  FEGPU_CUDA(cudaGetLastError());
+  FEGPU_CUDA(cudaMemcpyAsync(colptr, first.p, sizeof(int64_t) * (nc + 1), cudaMemcpyDeviceToHost, s));
+  FEGPU_CUDA(cudaMemcpyAsync(rowval, rv.p, sizeof(int64_t) * nnz, cudaMemcpyDeviceToHost, s));
+  FEGPU_CUDA(cudaMemcpyAsync(nzval, nz.p, sizeof(double) * nnz, cudaMemcpyDeviceToHost, s));
+  FEGPU_CUDA(cudaStreamSynchronize(s));
+  return nnz;
+}
+
+void transpose_values(const fegpu_dofmap *dm, const double *val, double *out, cudaStream_t s) {
+  const int64_t n = dm->ndof;
+  if (n <= 0) return;
+  k_transpose_vals<<<grid_of(n * 32), 256, 0, s>>>(dm->rowptr.as<int64_t>(),
+                                                   dm->colind.as<int32_t>(), val, n, out);
+  FEGPU_CUDA(cudaGetLastError());
+}
+
 void copy_csc(fegpu_context *ctx, const fegpu_dofmap *dm, const double *val, int drop_zeros,
               int64_t *colptr, int64_t *rowval, double *nzval) {
   cudaStream_t s = ctx->stream;
@@ -164,24 +292,16 @@ void copy_csc(fegpu_context *ctx, const fegpu_dofmap *dm, const double *val, int
 }
 
 }  // namespace fegpu
-
 // ---------------------------------------------------------------------------
 // Generic assembler: startassembly!/assemble!/makematrix! of
 // SysmatAssemblerSparse(Symm) (src/AssemblyModule.jl:209-329, 454-583) for
-// element matrices formed by the caller.  makematrix! runs on the device:
-// a stable radix sort of (column, row) keys keeps duplicates in input order,
-// and each run of equal keys is summed left to right, which is the
-// combine order of Julia's sparse(I, J, V).  The symmetric variant then forms
-// S + S' (exact zeros not stored) and halves the diagonal.
-struct fegpu_assembler {
-  fegpu_context *ctx = nullptr;
-  int symmetric = 0;
-  int64_t nrows = 0, ncols = 0;
-  std::vector<int64_t> I, J;
-  std::vector<double> V;
-  int64_t nnz = -1;
-  fegpu::DevBuf keys, vals;  // result: sorted unique keys (col << 32 | row), values
-};
+// element matrices formed by the caller.  makematrix! runs on the device: a
+// stable radix sort of (column, row) keys keeps duplicates in input order,
+// and each run of equal keys is summed left to right, which is the combine
+// order of Julia's sparse(I, J, V).  The symmetric variant then forms S + S'
+// (exact zeros not stored) and halves the diagonal.  Device forms that
+// produce rectangular COO data (bilform_masslike) hand their keys and values
+// to the same reduction.
 
 namespace fegpu {
 namespace {
@@ -193,6 +313,12 @@ __global__ void k_make_keys(const int64_t *I, const int64_t *J, int64_t n, uint6
     key[t] = (static_cast<uint64_t>(J[t] - 1) << 32) | static_cast<uint64_t>(I[t] - 1);
     idx[t] = t;
   }
+}
+
+__global__ void k_iota(int64_t n, int64_t *idx) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x)
+    idx[t] = t;
 }
 
 __global__ void k_heads(const uint64_t *key, int64_t n, int64_t *head) {
@@ -219,21 +345,24 @@ __global__ void k_reduce_runs(const uint64_t *key, const int64_t *order, const d
   }
 }
 
-// S + S': entries of S are tagged 0, mirrored entries 1; after a stable sort
-// a run is (S) or (S, S') or (S'): v = s + t with the missing one as 0.0.
+// S + S': entries of S are tagged 0..n-1, mirrored entries n..2n-1
 __global__ void k_mirror(const uint64_t *key, const double *val, int64_t n, uint64_t *k2,
-                         double *v2) {
+                         double *v2, int64_t *tag) {
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
        t += (int64_t)gridDim.x * blockDim.x) {
     const uint64_t c = key[t] >> 32, r = key[t] & 0xffffffffu;
     k2[t] = key[t];
     v2[t] = val[t];
+    tag[t] = t;
     k2[n + t] = (r << 32) | c;
     v2[n + t] = val[t];
+    tag[n + t] = n + t;
   }
 }
 
-__global__ void k_symm_runs(const uint64_t *key, const double *val, const int64_t *order,
+// after the stable sort a run is (S) or (S, S') or (S'): v = s + t with the
+// missing one as 0.0; exact zeros are not kept, the diagonal is halved
+__global__ void k_symm_runs(const uint64_t *key, const double *v2, const int64_t *order,
                             int64_t n2, int64_t nS, uint64_t *okey, double *oval, int64_t *keep) {
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n2;
        t += (int64_t)gridDim.x * blockDim.x) {
@@ -242,8 +371,8 @@ __global__ void k_symm_runs(const uint64_t *key, const double *val, const int64_
     double sv = 0.0, tv = 0.0;
     bool hs = false, ht = false;
     for (int64_t u = t; u < n2 && key[u] == key[t]; ++u) {
-      if (order[u] < nS) { sv = val[u]; hs = true; }
-      else { tv = val[u]; ht = true; }
+      if (order[u] < nS) { sv = v2[order[u]]; hs = true; }
+      else { tv = v2[order[u]]; ht = true; }
     }
     double v = hs && ht ? sv + tv : (hs ? sv + 0.0 : 0.0 + tv);
     const uint64_t c = key[t] >> 32, r = key[t] & 0xffffffffu;
@@ -256,23 +385,151 @@ __global__ void k_symm_runs(const uint64_t *key, const double *val, const int64_
   }
 }
 
+__global__ void k_scatter_kept(const uint64_t *okey, const double *oval, const int64_t *keep,
+                               const int64_t *pos, int64_t n, uint64_t *key, double *val) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x)
+    if (keep[t]) {
+      key[pos[t]] = okey[t];
+      val[pos[t]] = oval[t];
+    }
+}
+
+// CSC export: colptr[c] = 1 + (first entry of a column >= c), rows 1-based
+__global__ void k_colptr(const uint64_t *key, int64_t nnz, int64_t ncols, int64_t *colptr) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c <= ncols;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    int64_t lo = 0, hi = nnz;
+    const uint64_t target = static_cast<uint64_t>(c) << 32;
+    while (lo < hi) {
+      const int64_t mid = (lo + hi) >> 1;
+      if (key[mid] < target) lo = mid + 1;
+      else hi = mid;
+    }
+    colptr[c] = lo + 1;
+  }
+}
+
+__global__ void k_rowval(const uint64_t *key, int64_t nnz, int64_t *rowval) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nnz;
+       t += (int64_t)gridDim.x * blockDim.x)
+    rowval[t] = static_cast<int64_t>(key[t] & 0xffffffffu) + 1;
+}
+
+int key_bits(int64_t ncols) {
+  int b = 0;
+  while (b < 32 && (int64_t(1) << b) < ncols) ++b;
+  return 32 + b;
+}
+
+int64_t read_count(const int64_t *a, const int64_t *b, cudaStream_t s) {
+  int64_t h[2] = {0, 0};
+  FEGPU_CUDA(cudaMemcpyAsync(&h[0], a, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  if (b) FEGPU_CUDA(cudaMemcpyAsync(&h[1], b, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  FEGPU_CUDA(cudaStreamSynchronize(s));
+  return h[0] + h[1];
+}
+
+// S + S' of the reduced entries in a->keys / a->vals (nu of them)
+int64_t symmetric_completion(fegpu_assembler *a, int64_t nu) {
+  fegpu_context *ctx = a->ctx;
+  cudaStream_t s = ctx->stream;
+  const int64_t n2 = 2 * nu;
+  DevBuf k2, v2, k3, o2, o3, okey, oval, keep, pos, tmp;
+  k2.alloc(sizeof(uint64_t) * n2);
+  v2.alloc(sizeof(double) * n2);
+  k3.alloc(sizeof(uint64_t) * n2);
+  o2.alloc(sizeof(int64_t) * n2);
+  o3.alloc(sizeof(int64_t) * n2);
+  okey.alloc(sizeof(uint64_t) * n2);
+  oval.alloc(sizeof(double) * n2);
+  keep.alloc(sizeof(int64_t) * (n2 + 1));
+  pos.alloc(sizeof(int64_t) * (n2 + 1));
+  k_mirror<<<grid_of(nu), 256, 0, s>>>(a->keys.as<uint64_t>(), a->vals.as<double>(), nu,
+                                       k2.as<uint64_t>(), v2.as<double>(), o2.as<int64_t>());
+  const int bits = std::max(key_bits(a->ncols), key_bits(a->nrows));
+  cub_call(ctx, tmp, [&](void *t, size_t &b) {
+    return cub::DeviceRadixSort::SortPairs(t, b, k2.as<uint64_t>(), k3.as<uint64_t>(),
+                                           o2.as<int64_t>(), o3.as<int64_t>(), n2, 0, bits, s);
+  });
+  FEGPU_CUDA(cudaMemsetAsync(keep.as<int64_t>() + n2, 0, sizeof(int64_t), s));
+  k_symm_runs<<<grid_of(n2), 256, 0, s>>>(k3.as<uint64_t>(), v2.as<double>(), o3.as<int64_t>(),
+                                           n2, nu, okey.as<uint64_t>(), oval.as<double>(),
+                                           keep.as<int64_t>());
+  cub_call(ctx, tmp, [&](void *t, size_t &b) {
+    return cub::DeviceScan::ExclusiveSum(t, b, keep.as<int64_t>(), pos.as<int64_t>(), n2 + 1, s);
+  });
+  const int64_t kept = read_count(pos.as<int64_t>() + n2, nullptr, s);
+  a->keys.alloc(sizeof(uint64_t) * (kept + 1));
+  a->vals.alloc(sizeof(double) * (kept + 1));
+  k_scatter_kept<<<grid_of(n2), 256, 0, s>>>(okey.as<uint64_t>(), oval.as<double>(),
+                                              keep.as<int64_t>(), pos.as<int64_t>(), n2,
+                                              a->keys.as<uint64_t>(), a->vals.as<double>());
+  FEGPU_CUDA(cudaGetLastError());
+  FEGPU_CUDA(cudaStreamSynchronize(s));
+  return kept;
+}
+
 }  // namespace
+
+int64_t assembler_reduce(fegpu_assembler *a, DevBuf &key, DevBuf &idx, const double *V,
+                         int64_t n) {
+  fegpu_context *ctx = a->ctx;
+  cudaStream_t s = ctx->stream;
+  int64_t nu = 0;
+  if (n > 0) {
+    DevBuf key2, idx2, head, seg, tmp;
+    key2.alloc(sizeof(uint64_t) * n);
+    idx2.alloc(sizeof(int64_t) * n);
+    head.alloc(sizeof(int64_t) * n);
+    seg.alloc(sizeof(int64_t) * n);
+    const int bits = key_bits(a->ncols);
+    cub_call(ctx, tmp, [&](void *t, size_t &b) {
+      return cub::DeviceRadixSort::SortPairs(t, b, key.as<uint64_t>(), key2.as<uint64_t>(),
+                                             idx.as<int64_t>(), idx2.as<int64_t>(), n, 0, bits, s);
+    });
+    k_heads<<<grid_of(n), 256, 0, s>>>(key2.as<uint64_t>(), n, head.as<int64_t>());
+    cub_call(ctx, tmp, [&](void *t, size_t &b) {
+      return cub::DeviceScan::ExclusiveSum(t, b, head.as<int64_t>(), seg.as<int64_t>(), n, s);
+    });
+    nu = read_count(seg.as<int64_t>() + n - 1, head.as<int64_t>() + n - 1, s);
+    a->keys.alloc(sizeof(uint64_t) * (nu + 1));
+    a->vals.alloc(sizeof(double) * (nu + 1));
+    k_reduce_runs<<<grid_of(n), 256, 0, s>>>(key2.as<uint64_t>(), idx2.as<int64_t>(), V,
+                                             seg.as<int64_t>(), n, a->keys.as<uint64_t>(),
+                                             a->vals.as<double>());
+    FEGPU_CUDA(cudaGetLastError());
+  }
+  if (a->symmetric && nu > 0) nu = symmetric_completion(a, nu);
+  FEGPU_CUDA(cudaStreamSynchronize(s));
+  a->nnz = nu;
+  a->I.clear();
+  a->J.clear();
+  a->V.clear();  // buffer pointer back to 1: ready for the next assembly
+  return nu;
+}
+
 }  // namespace fegpu
 
 using namespace fegpu;
 
 extern "C" {
 
-int fegpu_assembler_create(fegpu_context *ctx, int symmetric, int64_t nrows, int64_t ncols,
+int fegpu_assembler_create(fegpu_context *ctx, int kind, int64_t nrows, int64_t ncols,
                            fegpu_assembler **out) {
   try {
     if (!ctx || !out) throw Error{FEGPU_ERR_ARG, "null handle"};
-    if (symmetric && nrows != ncols) throw Error{FEGPU_ERR_ARG, "Row and column info do not agree"};
+    if (kind < FEGPU_ASM_SPARSE || kind > FEGPU_ASM_HRZ_LUMPING_SYMM)
+      throw Error{FEGPU_ERR_ARG, "unknown assembler kind"};
+    const int symmetric = kind == FEGPU_ASM_SPARSE_SYMM;
+    if (kind != FEGPU_ASM_SPARSE && nrows != ncols)
+      throw Error{FEGPU_ERR_ARG, "Row and column info do not agree"};
     if (nrows < 1 || ncols < 1 || nrows >= (int64_t(1) << 32) || ncols >= (int64_t(1) << 32))
       throw Error{FEGPU_ERR_ARG, "bad matrix size"};
     auto *a = new fegpu_assembler();
     a->ctx = ctx;
     a->symmetric = symmetric;
+    a->kind = kind;
     a->nrows = nrows;
     a->ncols = ncols;
     *out = a;
@@ -296,7 +553,32 @@ int fegpu_assembler_assemble(fegpu_assembler *a, const double *mat, int nr, int 
                              const int64_t *rows, const int64_t *cols) {
   try {
     if (!a || !mat || !rows || !cols) throw Error{FEGPU_ERR_ARG, "null handle"};
-    if (a->symmetric && nr != nc) throw Error{FEGPU_ERR_ARG, "Size mismatch"};
+    if (a->kind != FEGPU_ASM_SPARSE && nr != nc) throw Error{FEGPU_ERR_ARG, "Size mismatch"};
+    if (a->kind == FEGPU_ASM_SPARSE_DIAG || a->kind == FEGPU_ASM_HRZ_LUMPING_SYMM) {
+      // the element's diagonal (times, for HRZ, the element total -- column
+      // sums, then their sum -- over the diagonal total)
+      double ff = 1.0;
+      if (a->kind == FEGPU_ASM_HRZ_LUMPING_SYMM) {
+        double em2 = 0.0, dem2 = 0.0;
+        for (int j = 0; j < nc; ++j) {
+          double cs = 0.0;
+          for (int i = 0; i < nr; ++i) cs += mat[static_cast<size_t>(j) * nr + i];
+          em2 += cs;
+        }
+        for (int i = 0; i < nr; ++i) dem2 += mat[static_cast<size_t>(i) * nr + i];
+        ff = em2 / dem2;
+      }
+      for (int j = 0; j < nc; ++j) {
+        const int64_t dj = cols[j];
+        if (dj < 1) throw Error{FEGPU_ERR_ARG, "Column degree of freedom < 1"};
+        if (dj > a->ncols) throw Error{FEGPU_ERR_ARG, "Column degree of freedom > size"};
+        const double v = mat[static_cast<size_t>(j) * nr + j];
+        a->I.push_back(dj);
+        a->J.push_back(dj);
+        a->V.push_back(a->kind == FEGPU_ASM_HRZ_LUMPING_SYMM ? v * ff : v);
+      }
+      return FEGPU_OK;
+    }
     for (int j = 0; j < nc; ++j) {
       const int64_t dj = cols[j];
       if (dj < 1) throw Error{FEGPU_ERR_ARG, "Column degree of freedom < 1"};
@@ -327,111 +609,21 @@ int fegpu_assembler_make(fegpu_assembler *a, int64_t *nnz) {
     FEGPU_CUDA(cudaSetDevice(ctx->device));
     cudaStream_t s = ctx->stream;
     const int64_t n = static_cast<int64_t>(a->V.size());
-    DevBuf dI, dJ, dV, key, key2, idx, idx2, head, seg, tmp;
+    DevBuf dI, dJ, dV, key, idx;
     dI.alloc(sizeof(int64_t) * (n + 1));
     dJ.alloc(sizeof(int64_t) * (n + 1));
     dV.alloc(sizeof(double) * (n + 1));
     key.alloc(sizeof(uint64_t) * (n + 1));
-    key2.alloc(sizeof(uint64_t) * (n + 1));
     idx.alloc(sizeof(int64_t) * (n + 1));
-    idx2.alloc(sizeof(int64_t) * (n + 1));
-    head.alloc(sizeof(int64_t) * (n + 1));
-    seg.alloc(sizeof(int64_t) * (n + 1));
-    int64_t nu = 0;
     if (n > 0) {
       FEGPU_CUDA(cudaMemcpyAsync(dI.p, a->I.data(), sizeof(int64_t) * n, cudaMemcpyHostToDevice, s));
       FEGPU_CUDA(cudaMemcpyAsync(dJ.p, a->J.data(), sizeof(int64_t) * n, cudaMemcpyHostToDevice, s));
       FEGPU_CUDA(cudaMemcpyAsync(dV.p, a->V.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
       k_make_keys<<<grid_of(n), 256, 0, s>>>(dI.as<int64_t>(), dJ.as<int64_t>(), n,
                                              key.as<uint64_t>(), idx.as<int64_t>());
-      cub_call(ctx, tmp, [&](void *t, size_t &b) {
-        return cub::DeviceRadixSort::SortPairs(t, b, key.as<uint64_t>(), key2.as<uint64_t>(),
-                                               idx.as<int64_t>(), idx2.as<int64_t>(), n, 0, 64, s);
-      });
-      k_heads<<<grid_of(n), 256, 0, s>>>(key2.as<uint64_t>(), n, head.as<int64_t>());
-      cub_call(ctx, tmp, [&](void *t, size_t &b) {
-        return cub::DeviceScan::ExclusiveSum(t, b, head.as<int64_t>(), seg.as<int64_t>(), n, s);
-      });
-      int64_t last[2];
-      FEGPU_CUDA(cudaMemcpyAsync(&last[0], seg.as<int64_t>() + n - 1, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-      FEGPU_CUDA(cudaMemcpyAsync(&last[1], head.as<int64_t>() + n - 1, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-      FEGPU_CUDA(cudaStreamSynchronize(s));
-      nu = last[0] + last[1];
-      a->keys.alloc(sizeof(uint64_t) * (nu + 1));
-      a->vals.alloc(sizeof(double) * (nu + 1));
-      k_reduce_runs<<<grid_of(n), 256, 0, s>>>(key2.as<uint64_t>(), idx2.as<int64_t>(),
-                                               dV.as<double>(), seg.as<int64_t>(), n,
-                                               a->keys.as<uint64_t>(), a->vals.as<double>());
       FEGPU_CUDA(cudaGetLastError());
     }
-    if (a->symmetric && nu > 0) {
-      const int64_t n2 = 2 * nu;
-      DevBuf k2, v2, k3, v3, o2, o3, okey, oval, keep, pos;
-      k2.alloc(sizeof(uint64_t) * n2);
-      v2.alloc(sizeof(double) * n2);
-      k3.alloc(sizeof(uint64_t) * n2);
-      v3.alloc(sizeof(double) * n2);
-      o2.alloc(sizeof(int64_t) * n2);
-      o3.alloc(sizeof(int64_t) * n2);
-      okey.alloc(sizeof(uint64_t) * n2);
-      oval.alloc(sizeof(double) * n2);
-      keep.alloc(sizeof(int64_t) * (n2 + 1));
-      pos.alloc(sizeof(int64_t) * (n2 + 1));
-      k_mirror<<<grid_of(nu), 256, 0, s>>>(a->keys.as<uint64_t>(), a->vals.as<double>(), nu,
-                                           k2.as<uint64_t>(), v2.as<double>());
-      // order tags: S entries 0..nu-1, mirrored nu..2nu-1
-      std::vector<int64_t> iota(n2);
-      for (int64_t t = 0; t < n2; ++t) iota[t] = t;
-      FEGPU_CUDA(cudaMemcpyAsync(o2.p, iota.data(), sizeof(int64_t) * n2, cudaMemcpyHostToDevice, s));
-      cub_call(ctx, tmp, [&](void *t, size_t &b) {
-        return cub::DeviceRadixSort::SortPairs(t, b, k2.as<uint64_t>(), k3.as<uint64_t>(),
-                                               o2.as<int64_t>(), o3.as<int64_t>(), n2, 0, 64, s);
-      });
-      // gather values into sorted order
-      std::vector<int64_t> hord(n2);
-      std::vector<double> hv2(n2), hv3(n2);
-      FEGPU_CUDA(cudaMemcpyAsync(hord.data(), o3.p, sizeof(int64_t) * n2, cudaMemcpyDeviceToHost, s));
-      FEGPU_CUDA(cudaMemcpyAsync(hv2.data(), v2.p, sizeof(double) * n2, cudaMemcpyDeviceToHost, s));
-      FEGPU_CUDA(cudaStreamSynchronize(s));
-      for (int64_t t = 0; t < n2; ++t) hv3[t] = hv2[hord[t]];
-      FEGPU_CUDA(cudaMemcpyAsync(v3.p, hv3.data(), sizeof(double) * n2, cudaMemcpyHostToDevice, s));
-      k_symm_runs<<<grid_of(n2), 256, 0, s>>>(k3.as<uint64_t>(), v3.as<double>(), o3.as<int64_t>(),
-                                               n2, nu, okey.as<uint64_t>(), oval.as<double>(),
-                                               keep.as<int64_t>());
-      cub_call(ctx, tmp, [&](void *t, size_t &b) {
-        return cub::DeviceScan::ExclusiveSum(t, b, keep.as<int64_t>(), pos.as<int64_t>(), n2 + 1, s);
-      });
-      int64_t kept = 0;
-      std::vector<int64_t> hkeep(n2), hpos(n2 + 1);
-      std::vector<uint64_t> hk(n2);
-      std::vector<double> hv(n2);
-      FEGPU_CUDA(cudaMemcpyAsync(hkeep.data(), keep.p, sizeof(int64_t) * n2, cudaMemcpyDeviceToHost, s));
-      FEGPU_CUDA(cudaMemcpyAsync(hk.data(), okey.p, sizeof(uint64_t) * n2, cudaMemcpyDeviceToHost, s));
-      FEGPU_CUDA(cudaMemcpyAsync(hv.data(), oval.p, sizeof(double) * n2, cudaMemcpyDeviceToHost, s));
-      FEGPU_CUDA(cudaStreamSynchronize(s));
-      std::vector<uint64_t> ck;
-      std::vector<double> cv;
-      for (int64_t t = 0; t < n2; ++t)
-        if (hkeep[t]) {
-          ck.push_back(hk[t]);
-          cv.push_back(hv[t]);
-        }
-      kept = static_cast<int64_t>(ck.size());
-      a->keys.alloc(sizeof(uint64_t) * (kept + 1));
-      a->vals.alloc(sizeof(double) * (kept + 1));
-      if (kept > 0) {
-        FEGPU_CUDA(cudaMemcpyAsync(a->keys.p, ck.data(), sizeof(uint64_t) * kept, cudaMemcpyHostToDevice, s));
-        FEGPU_CUDA(cudaMemcpyAsync(a->vals.p, cv.data(), sizeof(double) * kept, cudaMemcpyHostToDevice, s));
-      }
-      FEGPU_CUDA(cudaStreamSynchronize(s));
-      nu = kept;
-    }
-    FEGPU_CUDA(cudaStreamSynchronize(s));
-    a->nnz = nu;
-    a->I.clear();
-    a->J.clear();
-    a->V.clear();  // buffer pointer back to 1: ready for the next assembly
-    *nnz = nu;
+    *nnz = assembler_reduce(a, key, idx, dV.as<double>(), n);
     return FEGPU_OK;
   } catch (const Error &e) {
     set_error(e.msg);
@@ -448,18 +640,21 @@ int fegpu_assembler_copy_csc(fegpu_assembler *a, int64_t *colptr, int64_t *rowva
     if (a->nnz < 0) throw Error{FEGPU_ERR_STATE, "makematrix! has not run"};
     fegpu_context *ctx = a->ctx;
     FEGPU_CUDA(cudaSetDevice(ctx->device));
-    std::vector<uint64_t> hk(a->nnz);
-    if (a->nnz > 0) {
-      FEGPU_CUDA(cudaMemcpy(hk.data(), a->keys.p, sizeof(uint64_t) * a->nnz, cudaMemcpyDeviceToHost));
-      FEGPU_CUDA(cudaMemcpy(nzval, a->vals.p, sizeof(double) * a->nnz, cudaMemcpyDeviceToHost));
+    cudaStream_t s = ctx->stream;
+    const int64_t nnz = a->nnz;
+    DevBuf cp, rv;
+    cp.alloc(sizeof(int64_t) * (a->ncols + 1));
+    rv.alloc(sizeof(int64_t) * (nnz + 1));
+    k_colptr<<<grid_of(a->ncols + 1), 256, 0, s>>>(a->keys.as<uint64_t>(), nnz, a->ncols,
+                                                   cp.as<int64_t>());
+    if (nnz > 0) k_rowval<<<grid_of(nnz), 256, 0, s>>>(a->keys.as<uint64_t>(), nnz, rv.as<int64_t>());
+    FEGPU_CUDA(cudaGetLastError());
+    FEGPU_CUDA(cudaMemcpyAsync(colptr, cp.p, sizeof(int64_t) * (a->ncols + 1), cudaMemcpyDeviceToHost, s));
+    if (nnz > 0) {
+      FEGPU_CUDA(cudaMemcpyAsync(rowval, rv.p, sizeof(int64_t) * nnz, cudaMemcpyDeviceToHost, s));
+      FEGPU_CUDA(cudaMemcpyAsync(nzval, a->vals.p, sizeof(double) * nnz, cudaMemcpyDeviceToHost, s));
     }
-    std::vector<int64_t> cnt(a->ncols + 1, 0);
-    for (int64_t t = 0; t < a->nnz; ++t) {
-      cnt[(hk[t] >> 32) + 1]++;
-      rowval[t] = static_cast<int64_t>(hk[t] & 0xffffffffu) + 1;
-    }
-    colptr[0] = 1;
-    for (int64_t c = 0; c < a->ncols; ++c) colptr[c + 1] = colptr[c] + cnt[c + 1];
+    FEGPU_CUDA(cudaStreamSynchronize(s));
     return FEGPU_OK;
   } catch (const Error &e) {
     set_error(e.msg);

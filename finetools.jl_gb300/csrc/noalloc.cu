@@ -76,6 +76,7 @@ extern "C" int fegpu_bilform_lin_elastic_noalloc(fegpu_matrix *K, const fegpu_co
                   "(fegpu_bilform_lin_elastic with FEGPU_MIXED builds the node-to-element "
                   "tables this entry point reads)"};
     void *base = scratch_address(ctx->device);  // first call on a device: symbol lookup
+    K->unsym = false;
     const int64_t E = fm->nelem;
     const int nne = fm->nne;
     const int nblk = nne * (nne + 1) / 2;
@@ -186,6 +187,7 @@ extern "C" int fegpu_bilform_lin_elastic_noalloc(fegpu_matrix *K, const fegpu_co
     g.cpoff = dm->contiguous ? nullptr : dm->cpoff.as<int64_t>();
     g.val = K->val.as<double>();
     g.maxdeg = dm->maxdeg;
+    await_export(K, s);
     const int64_t nch = static_cast<int64_t>(dm->na_chunk_nodes.size()) - 1;
     for (int64_t c = 0; c < nch; ++c) {
       a.e0 = c * chunk;

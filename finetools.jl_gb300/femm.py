@@ -21,6 +21,7 @@ import ctypes as C
 import weakref
 
 import numpy as np
+import scipy.sparse as sp
 
 from . import _native as nat
 from .assembly import SysmatAssemblerGPU, SysvecAssemblerGPU, _is_assembler
@@ -298,8 +299,72 @@ def bilform_dot(femm: FEMMBase, *args, m=3):
     dm = _prepare(femm, geom, u)
     keep = []
     coef = _coef(femm, geom, cf, keep)
+    if getattr(assembler, "lumping", None):
+        # SysmatAssemblerSparseDiag / HRZLumpingSymm: a diagonal matrix on the
+        # DOFs of the element set (explicit zeros kept, as sparse() does)
+        diag = np.empty(dm.ndof)
+        nat.check(nat.load().fegpu_bilform_dot_lumped(
+            dm.h, C.byref(coef), int(m), int(assembler.lumping == "hrz"), nat.ptr(diag)))
+        conn = femm.integdomain.fes.conn - 1
+        dofs = np.unique(u.dofnums[np.unique(conn)].ravel()) - 1
+        return assembler._post(sp.csc_matrix((diag[dofs], (dofs, dofs)),
+                                             shape=(dm.ndof, dm.ndof)))
     return assembler._run(dm, lambda h: nat.load().fegpu_bilform_dot(
         h, C.byref(coef), int(m), int(assembler.symmetric), assembler.precision_code))
+
+
+def bilform_convection(femm: FEMMBase, *args):
+    """K = int w u . grad(q) dV for a scalar field (src/FEMMBaseModule.jl:1583-1625):
+    bilform_convection(femm, [assembler], geom, u, Q, rhof) with u the velocity
+    NodalField; the reference's default assembler is SysmatAssemblerSparse
+    (unsymmetric), and rhof does not enter the reference's matrix."""
+    assembler, (geom, u, Q, rhof) = _split(args, 4)
+    assembler = assembler or SysmatAssemblerGPU(symmetric=False)
+    if assembler.symmetric:
+        raise ValueError("convection: the element matrix is unsymmetric "
+                         "(use SysmatAssemblerGPU(symmetric=False))")
+    dm = _prepare(femm, geom, Q)
+    vel = np.asfortranarray(u.values, dtype=np.float64)
+    return assembler._run(dm, lambda h: nat.load().fegpu_bilform_convection(
+        h, vel.shape[1], vel.ctypes.data))
+
+
+def bilform_div_grad(femm: FEMMBase, *args):
+    """K = int mu grad(w) : grad(u) dV (src/FEMMBaseModule.jl:1672-1723); the
+    reference's default assembler is SysmatAssemblerSparse (unsymmetric)."""
+    assembler, (geom, u, viscf) = _split(args, 3)
+    assembler = assembler or SysmatAssemblerGPU(symmetric=False)
+    dm = _prepare(femm, geom, u)
+    keep = []
+    coef = _coef(femm, geom, viscf, keep)
+    return assembler._run(dm, lambda h: nat.load().fegpu_bilform_div_grad(
+        h, C.byref(coef), assembler.precision_code))
+
+
+def bilform_masslike(femm: FEMMBase, *args, m=3):
+    """Rectangular "mass-like" matrix (src/FEMMBaseModule.jl:1865-1927):
+    bilform_masslike(femm, [assembler], geom, phi, cf; m=3) with nelem*ndn
+    rows (rows (i-1)*ndn+1 .. i*ndn belong to element i) and nalldofs(phi)
+    columns, M[(i-1)*ndn+p, dof(b,q)] = int N_b c[p,q].  The reference's
+    default assembler is SysmatAssemblerSparse: only an unsymmetric,
+    unlumped GPU assembler applies (the matrix is not square)."""
+    assembler, (geom, phi, cf) = _split(args, 3)
+    assembler = assembler or SysmatAssemblerGPU(symmetric=False)
+    inner = getattr(assembler, "_a", assembler)  # an FF-block assembler's wrapped one
+    if inner.symmetric or inner.lumping:
+        raise ValueError("masslike: the matrix is rectangular "
+                         "(use SysmatAssemblerGPU(symmetric=False))")
+    dm = _prepare(femm, geom, phi)
+    keep = []
+    coef = _coef(femm, geom, cf, keep)
+    if coef.kind == nat.COEF_ISO_LAME:
+        raise ValueError("masslike: the coefficient is a scalar or an ndn x ndn matrix")
+    nelem = femm.integdomain.fes.count()
+    inner._open_generic(nat.ASM_SPARSE, nelem * dm.ndn, dm.ndof)
+    nnz = C.c_int64()
+    nat.check(nat.load().fegpu_bilform_masslike(dm.h, C.byref(coef), int(m),
+                                                inner._generic, C.byref(nnz)))
+    return assembler._post(inner._generic_csc(nnz.value))
 
 
 def innerproduct(femm: FEMMBase, *args):

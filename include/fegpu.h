@@ -141,6 +141,16 @@ int fegpu_matrix_destroy(fegpu_matrix *K);
  * lower triangle by local index, mirrored), 0 reproduces SysmatAssemblerSparse. */
 int fegpu_bilform_diffusion(fegpu_matrix *K, const fegpu_coef *cf, int precision);
 int fegpu_bilform_lin_elastic(fegpu_matrix *K, const fegpu_coef *cf, int precision);
+/* bilform_convection: src/FEMMBaseModule.jl:1583-1625, scalar field (one DOF
+ * per node); velocity: nnodes x nsd column-major (NodalField values), nsd =
+ * the space = manifold dimension.  The reference's default assembler is
+ * SysmatAssemblerSparse (copy out with drop_zeros = 0); its density rhof
+ * does not enter the matrix and is not an argument. */
+int fegpu_bilform_convection(fegpu_matrix *K, int nsd, const double *velocity);
+/* bilform_div_grad: src/FEMMBaseModule.jl:1672-1723 (3-D, ndn = 3; scalar
+ * viscosity, constant or per element).  The reference's default assembler is
+ * SysmatAssemblerSparse: copy out with drop_zeros = 0. */
+int fegpu_bilform_div_grad(fegpu_matrix *K, const fegpu_coef *cf, int precision);
 int fegpu_bilform_dot(fegpu_matrix *K, const fegpu_coef *cf, int m, int symmetric,
                       int precision);
 
@@ -148,6 +158,14 @@ int fegpu_bilform_dot(fegpu_matrix *K, const fegpu_coef *cf, int m, int symmetri
  * vector, SysvecAssembler semantics (src/AssemblyModule.jl:853-917).
  * f: ncomp = ndn.  F: nalldofs doubles (host). */
 int fegpu_linform_dot(fegpu_dofmap *dm, const fegpu_coef *f, int m, double *F);
+/* bilform_dot assembled by SysmatAssemblerSparseDiag (hrz = 0,
+ * src/AssemblyModule.jl:722-750) or SysmatAssemblerSparseHRZLumpingSymm
+ * (hrz = 1, src/AssemblyModule.jl:1065-1095): the diagonal of the lumped
+ * matrix (nalldofs values; the matrix is diag(diag) on the DOFs of the
+ * element set).  Coefficient: scalar (constant, per element, per point) or a
+ * constant ndn x ndn matrix. */
+int fegpu_bilform_dot_lumped(fegpu_dofmap *dm, const fegpu_coef *f, int m, int hrz,
+                             double *diag);
 
 /* makematrix! output.  drop_zeros = 1 leaves out entries that are exactly
  * zero, as the S + transpose(S) step of SysmatAssemblerSparseSymm does
@@ -158,6 +176,27 @@ int fegpu_matrix_copy_csc(fegpu_matrix *K, int drop_zeros, int64_t *colptr,
                           int64_t *rowval, double *nzval);
 /* values only, in the structural pattern order (re-assembly on a fixed mesh) */
 int fegpu_matrix_copy_values(fegpu_matrix *K, double *nzval);
+/* The same copy without waiting for it: queued on the context's export
+ * stream behind the work already queued for K, it overlaps what the caller
+ * queues next (the next assembly into another matrix, a coordinate upload).
+ * nzval should be page-locked host memory and stays in use until
+ * fegpu_matrix_wait_export(K) returns.  A form that writes K again waits on
+ * the device for the copy first, so two matrices of one dofmap used in turn
+ * pipeline the assembly of one with the export of the other. */
+int fegpu_matrix_copy_values_async(fegpu_matrix *K, double *nzval);
+int fegpu_matrix_wait_export(fegpu_matrix *K);
+/* A block of the matrix as CSC (1-based, (row1-row0) x (col1-col0)): rows
+ * [row0, row1) x columns [col0, col1), 0-based half-open -- matrix_blocked_ff
+ * / _fd / _df / _dd and the makematrix! of SysmatAssemblerFFBlock
+ * (src/MatrixUtilityModule.jl:675-806, src/AssemblyModule.jl:1229-1236) with
+ * the free DOFs numbered first.  drop_zeros = 0 keeps the stored entries
+ * (explicit zeros included: a SysmatAssemblerSparse matrix), 1 leaves out
+ * exact zeros (a SysmatAssemblerSparseSymm matrix, whose S + S' stores
+ * none).  Call with colptr = rowval = nzval = NULL for the entry count, then
+ * again with arrays of (col1 - col0 + 1) and *nnz entries. */
+int fegpu_matrix_copy_block_csc(fegpu_matrix *K, int64_t row0, int64_t row1, int64_t col0,
+                                int64_t col1, int drop_zeros, int64_t *nnz, int64_t *colptr,
+                                int64_t *rowval, double *nzval);
 /* y = K x on the device (host vectors of length nalldofs) */
 int fegpu_matrix_spmv(fegpu_matrix *K, const double *x, double *y);
 /* conjugategradient(K, b, x0, maxiter) (src/AlgoBaseModule.jl:425-445): the
@@ -265,8 +304,16 @@ int fegpu_server_memory(fegpu_server *s, int64_t *free_bytes, int64_t *total_byt
  * startassembly! / assemble! / makematrix! of SysmatAssemblerSparse(Symm)
  * (src/AssemblyModule.jl:209-329, 454-583) for FEMMs whose element matrices
  * are computed by the caller: triples are buffered on the host, then sorted
- * and reduced on the device into CSC (duplicates summed in input order). */
-int fegpu_assembler_create(fegpu_context *ctx, int symmetric, int64_t nrows,
+ * and reduced on the device into CSC (duplicates summed in input order).
+ * kind: 0 SysmatAssemblerSparse, 1 SysmatAssemblerSparseSymm,
+ * 2 SysmatAssemblerSparseDiag (element diagonals, src/AssemblyModule.jl:
+ * 722-750), 3 SysmatAssemblerSparseHRZLumpingSymm (diagonals scaled by the
+ * element total over the diagonal total, 1065-1095). */
+#define FEGPU_ASM_SPARSE 0
+#define FEGPU_ASM_SPARSE_SYMM 1
+#define FEGPU_ASM_SPARSE_DIAG 2
+#define FEGPU_ASM_HRZ_LUMPING_SYMM 3
+int fegpu_assembler_create(fegpu_context *ctx, int kind, int64_t nrows,
                            int64_t ncols, fegpu_assembler **out);
 int fegpu_assembler_destroy(fegpu_assembler *a);
 int fegpu_assembler_assemble(fegpu_assembler *a, const double *mat_colmajor,
@@ -275,6 +322,19 @@ int fegpu_assembler_assemble(fegpu_assembler *a, const double *mat_colmajor,
 int fegpu_assembler_make(fegpu_assembler *a, int64_t *nnz);
 int fegpu_assembler_copy_csc(fegpu_assembler *a, int64_t *colptr,
                              int64_t *rowval, double *nzval);
+
+/* bilform_masslike (src/FEMMBaseModule.jl:1865-1917): the rectangular matrix
+ * of nelem*ndn rows (rows (i-1)*ndn+1 .. i*ndn belong to element i, element
+ * order) and nalldofs columns, M[(i-1)*ndn+p, dof(b,q)] = sum N_b Jac w c[p,q]
+ * with Jac = Jacobianmdim(m).  The element blocks are formed on the device
+ * and reduced into `a`, which must be a FEGPU_ASM_SPARSE assembler of size
+ * nelem*ndn x nalldofs (the reference's default SysmatAssemblerSparse; its
+ * startassembly! drops triples assembled before).  c: constant, per element
+ * or per quadrature point (element order); a scalar or ndn x ndn row-major.
+ * Afterwards the assembler holds the made matrix: *nnz entries, copied out
+ * with fegpu_assembler_copy_csc. */
+int fegpu_bilform_masslike(fegpu_dofmap *dm, const fegpu_coef *cf, int m,
+                           fegpu_assembler *a, int64_t *nnz);
 
 #ifdef __cplusplus
 }

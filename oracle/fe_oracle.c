@@ -44,10 +44,11 @@ int orc_nodesperelem(int et) {
     case ORC_H20: return 20;
     case ORC_T4: return 4;
     case ORC_T10: return 10;
+    case ORC_L2: return 2;
   }
   return 0;
 }
-int orc_manifdim(int et) { return et == ORC_Q4 ? 2 : 3; }
+int orc_manifdim(int et) { return et == ORC_L2 ? 1 : (et == ORC_Q4 ? 2 : 3); }
 
 /* ------------------------------------------------------------------ */
 /* Integration rules: GaussRule src/IntegRuleModule.jl:193-398         */
@@ -118,7 +119,10 @@ int orc_tet_rule(int npts, double *pc, double *w) {
 /* 713-733, H8 955-992, H20 1030-1179, T4 1344-1364, T10 1395-1427.     */
 /* ------------------------------------------------------------------ */
 void orc_bfun(int et, const double *p, double *N) {
-  if (et == ORC_Q4) {
+  if (et == ORC_L2) { /* src/FESetModule.jl:592-594 */
+    N[0] = (1.0 - p[0]) / 2.0;
+    N[1] = (1.0 + p[0]) / 2.0;
+  } else if (et == ORC_Q4) {
     double x = p[0], y = p[1];
     N[0] = 0.25 * (1.0 - x) * (1.0 - y);
     N[1] = 0.25 * (1.0 + x) * (1.0 - y);
@@ -182,7 +186,10 @@ void orc_bfun(int et, const double *p, double *N) {
 }
 
 void orc_bfundpar(int et, const double *p, double *d) {
-  if (et == ORC_Q4) {
+  if (et == ORC_L2) { /* src/FESetModule.jl:595 */
+    d[0] = -1.0 / 2.0;
+    d[1] = 1.0 / 2.0;
+  } else if (et == ORC_Q4) {
     double x = p[0], y = p[1];
     d[0] = -(1.0 - y) * 0.25; d[1] = -(1.0 - x) * 0.25;
     d[2] = (1.0 - y) * 0.25;  d[3] = -(1.0 + x) * 0.25;
@@ -516,6 +523,7 @@ struct orc_matrix {
 
 int64_t orc_matrix_nnz(const orc_matrix *a) { return a->nnz; }
 int64_t orc_matrix_nrows(const orc_matrix *a) { return a->m; }
+int64_t orc_matrix_ncols(const orc_matrix *a) { return a->n; }
 int64_t orc_matrix_zeros_dropped(const orc_matrix *a) { return a->zeros_dropped; }
 void orc_matrix_copy(const orc_matrix *a, int64_t *colptr, int64_t *rowval,
                      double *nzval) {
@@ -687,8 +695,35 @@ static void asm_reserve(orc_assembler *a, int64_t extra) {
  * index, i >= j, column by column (500-533).  Same bounds checks. */
 int orc_assembler_assemble(orc_assembler *a, const double *mat, int nr, int nc,
                            const int64_t *rows, const int64_t *cols) {
-  if (a->kind == ORC_ASM_SPARSE_SYMM && nr != nc) { set_err("Size mismatch"); return -1; }
+  if (a->kind != ORC_ASM_SPARSE && nr != nc) { set_err("Size mismatch"); return -1; }
   asm_reserve(a, (int64_t)nr * nc);
+  if (a->kind == ORC_ASM_DIAG || a->kind == ORC_ASM_HRZ) {
+    /* assemble! of the diagonal assemblers (src/AssemblyModule.jl:722-750,
+     * 1065-1095): the element matrix's diagonal, for HRZ scaled by the
+     * element's total (column sums, then their sum) over its diagonal sum */
+    double ffactor = 1.0;
+    if (a->kind == ORC_ASM_HRZ) {
+      double em2 = 0.0, dem2 = 0.0;
+      for (int j = 0; j < nc; ++j) {
+        double cs = 0.0;
+        for (int i = 0; i < nr; ++i) cs += mat[(size_t)i * nc + j];
+        em2 += cs;
+      }
+      for (int i = 0; i < nr; ++i) dem2 += mat[(size_t)i * nc + i];
+      ffactor = em2 / dem2;
+    }
+    for (int j = 0; j < nc; ++j) {
+      int64_t dj = cols[j];
+      if (dj < 1) { set_err("Column degree of freedom < 1"); return -1; }
+      if (dj > a->ncols) { set_err("Column degree of freedom > size"); return -1; }
+      a->I[a->len] = dj;
+      a->J[a->len] = dj;
+      a->V[a->len] = a->kind == ORC_ASM_HRZ ? mat[(size_t)j * nc + j] * ffactor
+                                            : mat[(size_t)j * nc + j];
+      a->len++;
+    }
+    return 0;
+  }
   for (int j = 0; j < nc; ++j) {
     int64_t dj = cols[j];
     if (dj < 1) { set_err("Column degree of freedom < 1"); return -1; }
@@ -750,9 +785,15 @@ static void locjac(int nne, int sdim, int mdim, const double *X, const double *N
     }
 }
 
-/* Jacobian (src/FESetModule.jl:426-435 two-manifold, 479-489 three-manifold) */
+/* Jacobian (src/FESetModule.jl:387-391 one-manifold, 426-435 two-manifold,
+ * 479-489 three-manifold) */
 static double jac_det(int sdim, int mdim, const double *J) {
 #define JJ(r, c) J[((r) - 1) * mdim + ((c) - 1)]
+  if (mdim == 1) {
+    double s = 0.0;
+    for (int r = 1; r <= sdim; ++r) s += JJ(r, 1) * JJ(r, 1);
+    return sqrt(s);
+  }
   if (mdim == 3) {
     return JJ(1, 1) * (JJ(2, 2) * JJ(3, 3) - JJ(3, 2) * JJ(2, 3)) -
            JJ(1, 2) * (JJ(2, 1) * JJ(3, 3) - JJ(2, 3) * JJ(3, 1)) +
@@ -827,11 +868,13 @@ static const double *coef_at(const orc_coef *c, int64_t e, int q, int npts) {
   return c->data + ((size_t)e * npts + q) * c->ncomp;
 }
 
-/* Jacobianmdim / Jacobianvolume (src/IntegDomainModule.jl:504-549, 567-602):
- * a two-manifold integrated as a volume is scaled by the other dimension. */
+/* Jacobianmdim / Jacobianvolume (src/IntegDomainModule.jl:370-383, 405-450,
+ * 504-549, 567-602): a two-manifold integrated as a volume, and a curve
+ * integrated as a surface or a volume, are scaled by the other dimension. */
 static double jac_mdim(const orc_problem *p, int mdim, const double *J, int m) {
   double d = jac_det(p->sdim, mdim, J);
   if (mdim == 2 && m == 3) return d * p->otherdim;
+  if (mdim == 1 && m >= 2) return d * p->otherdim;
   return d;
 }
 
@@ -851,6 +894,9 @@ orc_matrix *orc_bilform(const orc_problem *p, int form, const orc_coef *c, int m
     set_err("diffusion: the manifold must fill the space"); return NULL;
   }
   if (form == ORC_DOT && c->ncomp != ndn * ndn) { set_err("dot: ndn x ndn coefficient"); return NULL; }
+  if (form == ORC_DIV_GRAD && (c->ncomp != 1 || ndn != mdim || mdim != sdim)) {
+    set_err("div_grad: scalar viscosity, ndn = mdim = sdim"); return NULL;
+  }
   double *Ns = (double *)malloc(sizeof(double) * npts * nne);
   double *dNs = (double *)malloc(sizeof(double) * npts * nne * mdim);
   for (int q = 0; q < npts; ++q) {
@@ -925,6 +971,22 @@ orc_matrix *orc_bilform(const orc_problem *p, int form, const orc_coef *c, int m
             for (int px = 0; px < 6; ++px) acc += B[px * n + mx] * DB[px * n + nx];
             Ke[mx * n + nx] += acc;
           }
+      } else if (form == ORC_DIV_GRAD) {
+        /* bilform_div_grad, src/FEMMBaseModule.jl:1690-1710 (full matrix) */
+        double Jac = jac_mdim(p, mdim, J, 3);
+        grad_n(nne, mdim, dN, J, g);
+        double factor = cv[0] * (Jac * p->w[q]);
+        for (int aa = 0; aa < nne; ++aa)
+          for (int bb = 0; bb < nne; ++bb)
+            for (int s = 0; s < ndn; ++s) {
+              int pr = aa * ndn + s, rc = bb * ndn + s;
+              for (int qq = 0; qq < ndn; ++qq)
+                Ke[pr * n + rc] += factor * g[aa * mdim + qq] * g[bb * mdim + qq];
+              for (int qq = 0; qq < ndn; ++qq) {
+                rc = bb * ndn + qq;
+                Ke[pr * n + rc] += factor * g[aa * mdim + qq] * g[bb * mdim + s];
+              }
+            }
       } else { /* ORC_DOT, src/FEMMBaseModule.jl:1348-1364 */
         double Jac = jac_mdim(p, mdim, J, m);
         for (int k = 0; k < nne; ++k)
@@ -936,7 +998,7 @@ orc_matrix *orc_bilform(const orc_problem *p, int form, const orc_coef *c, int m
           }
       }
     }
-    if (form != ORC_DOT) /* complete_lt! (src/MatrixUtilityModule.jl:164-173) */
+    if (form != ORC_DOT && form != ORC_DIV_GRAD) /* complete_lt! (src/MatrixUtilityModule.jl:164-173) */
       for (int nx = 0; nx < n; ++nx)
         for (int mx = nx + 1; mx < n; ++mx) Ke[mx * n + nx] = Ke[nx * n + mx];
     /* gatherdofnums! (src/FieldModule.jl:304-314): node-major order */
@@ -954,6 +1016,118 @@ orc_matrix *orc_bilform(const orc_problem *p, int form, const orc_coef *c, int m
   orc_assembler_free(a);
   free(Ns); free(dNs); free(X); free(Ke); free(g); free(B); free(DB); free(kg); free(dofs);
   return K;
+}
+
+/* bilform_convection (src/FEMMBaseModule.jl:1583-1625) into
+ * SysmatAssemblerSparse: K[p, r] += N_p (u . grad N_r) Jac w with u the
+ * interpolated velocity (nnodes x nsd, row-major here); the density rhof is
+ * evaluated by the reference but does not enter the matrix.  Scalar field. */
+orc_matrix *orc_bilform_convection(const orc_problem *p, const double *vel, int nsd) {
+  int nne = orc_nodesperelem(p->etype), mdim = orc_manifdim(p->etype);
+  int sdim = p->sdim, npts = p->npts;
+  if (p->ndn != 1) { set_err("convection: scalar field"); return NULL; }
+  if (mdim != sdim || nsd != sdim) { set_err("convection: nsd = sdim = mdim"); return NULL; }
+  double *Ns = (double *)malloc(sizeof(double) * npts * nne);
+  double *dNs = (double *)malloc(sizeof(double) * npts * nne * mdim);
+  for (int q = 0; q < npts; ++q) {
+    orc_bfun(p->etype, p->pc + q * mdim, Ns + q * nne);
+    orc_bfundpar(p->etype, p->pc + q * mdim, dNs + q * nne * mdim);
+  }
+  double *X = (double *)malloc(sizeof(double) * nne * sdim);
+  double *U = (double *)malloc(sizeof(double) * nne * nsd);
+  double *Ke = (double *)malloc(sizeof(double) * nne * nne);
+  double *g = (double *)malloc(sizeof(double) * nne * mdim);
+  int64_t *dofs = (int64_t *)malloc(sizeof(int64_t) * nne);
+  double loc[3], J[9];
+  orc_assembler *a = orc_assembler_create(ORC_ASM_SPARSE, p->nalldofs, p->nalldofs);
+  asm_reserve(a, p->nelem * (int64_t)nne * nne);
+  for (int64_t e = 0; e < p->nelem; ++e) {
+    const int64_t *ce = p->conn + (size_t)e * nne;
+    for (int k = 0; k < nne; ++k) {
+      for (int d = 0; d < sdim; ++d) X[k * sdim + d] = p->xyz[(size_t)(ce[k] - 1) * sdim + d];
+      for (int d = 0; d < nsd; ++d) U[k * nsd + d] = vel[(size_t)(ce[k] - 1) * nsd + d];
+    }
+    memset(Ke, 0, sizeof(double) * nne * nne);
+    for (int q = 0; q < npts; ++q) {
+      const double *N = Ns + q * nne, *dN = dNs + q * nne * mdim;
+      locjac(nne, sdim, mdim, X, N, dN, loc, J);
+      double Jac = jac_mdim(p, mdim, J, 3);
+      grad_n(nne, mdim, dN, J, g);
+      for (int pp = 0; pp < nne; ++pp)
+        for (int r = 0; r < nne; ++r) {
+          double accum = 0.0;
+          for (int s = 0; s < nsd; ++s) {
+            double u_s = 0.0;
+            for (int k = 0; k < nne; ++k) u_s += N[k] * U[k * nsd + s];
+            accum += u_s * g[r * mdim + s];
+          }
+          Ke[pp * nne + r] += N[pp] * accum * (Jac * p->w[q]);
+        }
+    }
+    for (int k = 0; k < nne; ++k) dofs[k] = p->dofnums[(size_t)(ce[k] - 1)];
+    if (orc_assembler_assemble(a, Ke, nne, nne, dofs, dofs) != 0) {
+      orc_assembler_free(a);
+      return NULL;
+    }
+  }
+  orc_matrix *K = orc_assembler_make(a);
+  orc_assembler_free(a);
+  free(Ns); free(dNs); free(X); free(U); free(Ke); free(g); free(dofs);
+  return K;
+}
+
+/* bilform_masslike (src/FEMMBaseModule.jl:1865-1917) into
+ * SysmatAssemblerSparse: a rectangular matrix of nelem*ndn rows (the ndn
+ * rows of element i are (i-1)*ndn+1 .. i*ndn) and nalldofs columns; element
+ * block M[p, (b-1)*ndn + q] += N_b Jac w c[p, q], Jac = Jacobianmdim(m). */
+orc_matrix *orc_bilform_masslike(const orc_problem *p, const orc_coef *c, int m) {
+  int nne = orc_nodesperelem(p->etype), mdim = orc_manifdim(p->etype);
+  int sdim = p->sdim, ndn = p->ndn, npts = p->npts;
+  int nc = nne * ndn;
+  if (mdim == 3 && m != 3) { set_err("That is the only acceptable option here."); return NULL; }
+  if (c->ncomp != ndn * ndn) { set_err("masslike: ndn x ndn coefficient"); return NULL; }
+  double *Ns = (double *)malloc(sizeof(double) * npts * nne);
+  double *dNs = (double *)malloc(sizeof(double) * npts * nne * mdim);
+  for (int q = 0; q < npts; ++q) {
+    orc_bfun(p->etype, p->pc + q * mdim, Ns + q * nne);
+    orc_bfundpar(p->etype, p->pc + q * mdim, dNs + q * nne * mdim);
+  }
+  double *X = (double *)malloc(sizeof(double) * nne * sdim);
+  double *Me = (double *)malloc(sizeof(double) * ndn * nc);
+  int64_t *rows = (int64_t *)malloc(sizeof(int64_t) * ndn);
+  int64_t *dofs = (int64_t *)malloc(sizeof(int64_t) * nc);
+  double loc[3], J[9];
+  orc_assembler *a = orc_assembler_create(ORC_ASM_SPARSE, p->nelem * ndn, p->nalldofs);
+  if (!a) return NULL;
+  asm_reserve(a, p->nelem * (int64_t)ndn * nc);
+  for (int64_t e = 0; e < p->nelem; ++e) {
+    const int64_t *ce = p->conn + (size_t)e * nne;
+    for (int k = 0; k < nne; ++k)
+      for (int d = 0; d < sdim; ++d) X[k * sdim + d] = p->xyz[(size_t)(ce[k] - 1) * sdim + d];
+    memset(Me, 0, sizeof(double) * ndn * nc);
+    for (int q = 0; q < npts; ++q) {
+      const double *N = Ns + q * nne, *dN = dNs + q * nne * mdim;
+      locjac(nne, sdim, mdim, X, N, dN, loc, J);
+      double Jac = jac_mdim(p, mdim, J, m);
+      const double *cv = coef_at(c, e, q, npts);
+      for (int b = 0; b < nne; ++b) {
+        double factor = N[b] * Jac * p->w[q];
+        for (int pp = 0; pp < ndn; ++pp)
+          for (int qq = 0; qq < ndn; ++qq) Me[pp * nc + b * ndn + qq] += factor * cv[pp * ndn + qq];
+      }
+    }
+    for (int k = 0; k < nne; ++k)
+      for (int d = 0; d < ndn; ++d) dofs[k * ndn + d] = p->dofnums[(size_t)(ce[k] - 1) * ndn + d];
+    for (int pp = 0; pp < ndn; ++pp) rows[pp] = e * ndn + pp + 1;
+    if (orc_assembler_assemble(a, Me, ndn, nc, rows, dofs) != 0) {
+      orc_assembler_free(a);
+      return NULL;
+    }
+  }
+  orc_matrix *M = orc_assembler_make(a);
+  orc_assembler_free(a);
+  free(Ns); free(dNs); free(X); free(Me); free(rows); free(dofs);
+  return M;
 }
 
 /* linform_dot (src/FEMMBaseModule.jl:1207-1244) into SysvecAssembler

@@ -27,10 +27,15 @@
 extern "C" {
 #endif
 
-enum { ORC_Q4 = 0, ORC_H8 = 1, ORC_H20 = 2, ORC_T4 = 3, ORC_T10 = 4 };
-enum { ORC_DIFFUSION = 0, ORC_LIN_ELASTIC = 1, ORC_DOT = 2 };
+/* ORC_L2 (two-node line, src/FESetModule.jl:590-595) is an oracle-only type:
+ * it runs the reference's one-dimensional known-answer tests. */
+enum { ORC_Q4 = 0, ORC_H8 = 1, ORC_H20 = 2, ORC_T4 = 3, ORC_T10 = 4, ORC_L2 = 5 };
+enum { ORC_DIFFUSION = 0, ORC_LIN_ELASTIC = 1, ORC_DOT = 2, ORC_DIV_GRAD = 3 };
 enum { ORC_COEF_CONST = 0, ORC_COEF_PER_ELEMENT = 1, ORC_COEF_PER_QP = 2 };
-enum { ORC_ASM_SPARSE = 0, ORC_ASM_SPARSE_SYMM = 1 };
+/* SysmatAssemblerSparse, SysmatAssemblerSparseSymm, SysmatAssemblerSparseDiag,
+ * SysmatAssemblerSparseHRZLumpingSymm (src/AssemblyModule.jl:88-329, 342-583,
+ * 599-794, 943-1145) */
+enum { ORC_ASM_SPARSE = 0, ORC_ASM_SPARSE_SYMM = 1, ORC_ASM_DIAG = 2, ORC_ASM_HRZ = 3 };
 
 typedef struct {
   int etype;
@@ -90,6 +95,7 @@ int64_t orc_element_coloring(int64_t nelem, int nne, const int64_t *conn,
 typedef struct orc_matrix orc_matrix;
 int64_t orc_matrix_nnz(const orc_matrix *m);
 int64_t orc_matrix_nrows(const orc_matrix *m);
+int64_t orc_matrix_ncols(const orc_matrix *m);
 int64_t orc_matrix_zeros_dropped(const orc_matrix *m);
 void orc_matrix_copy(const orc_matrix *m, int64_t *colptr, int64_t *rowval,
                      double *nzval);
@@ -108,6 +114,9 @@ void orc_assembler_free(orc_assembler *a);
 orc_matrix *orc_bilform(const orc_problem *p, int form, const orc_coef *c,
                         int m, int asm_kind, double *phase_seconds);
 int orc_linform_dot(const orc_problem *p, const orc_coef *f, int m, double *F);
+orc_matrix *orc_bilform_convection(const orc_problem *p, const double *vel, int nsd);
+/* bilform_masslike (src/FEMMBaseModule.jl:1865-1917): nelem*ndn x nalldofs */
+orc_matrix *orc_bilform_masslike(const orc_problem *p, const orc_coef *c, int m);
 const char *orc_last_error(void);
 
 /* CSR node-adjacency degrees (connectionmatrix, src/FEMMBaseModule.jl:490-510) */

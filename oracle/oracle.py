@@ -21,9 +21,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIBPATH = os.path.join(HERE, "_build", "libfe_oracle.so")
 
 Q4, H8, H20, T4, T10 = 0, 1, 2, 3, 4
-DIFFUSION, LIN_ELASTIC, DOT = 0, 1, 2
+L2 = 5  # oracle-only two-node line (runs the reference's 1-D known-answer tests)
+DIFFUSION, LIN_ELASTIC, DOT, DIV_GRAD = 0, 1, 2, 3
 COEF_CONST, COEF_PER_ELEMENT, COEF_PER_QP = 0, 1, 2
-ASM_SPARSE, ASM_SPARSE_SYMM = 0, 1
+ASM_SPARSE, ASM_SPARSE_SYMM, ASM_DIAG, ASM_HRZ = 0, 1, 2, 3
 NNE = {Q4: 4, H8: 8, H20: 20, T4: 4, T10: 10}
 MDIM = {Q4: 2, H8: 3, H20: 3, T4: 3, T10: 3}
 
@@ -78,6 +79,8 @@ def lib():
     L.orc_matrix_nnz.restype = i64
     L.orc_matrix_nrows.argtypes = [vp]
     L.orc_matrix_nrows.restype = i64
+    L.orc_matrix_ncols.argtypes = [vp]
+    L.orc_matrix_ncols.restype = i64
     L.orc_matrix_zeros_dropped.argtypes = [vp]
     L.orc_matrix_zeros_dropped.restype = i64
     L.orc_matrix_copy.argtypes = [vp, vp, vp, vp]
@@ -91,6 +94,10 @@ def lib():
     L.orc_bilform.argtypes = [C.POINTER(_Problem), i32, C.POINTER(_Coef), i32, i32, vp]
     L.orc_bilform.restype = vp
     L.orc_linform_dot.argtypes = [C.POINTER(_Problem), C.POINTER(_Coef), i32, vp]
+    L.orc_bilform_convection.argtypes = [C.POINTER(_Problem), vp, i32]
+    L.orc_bilform_convection.restype = vp
+    L.orc_bilform_masslike.argtypes = [C.POINTER(_Problem), C.POINTER(_Coef), i32]
+    L.orc_bilform_masslike.restype = vp
     L.orc_last_error.restype = C.c_char_p
     _lib = L
     return L
@@ -219,7 +226,8 @@ def _take_matrix(h):
     L = lib()
     if not h:
         raise RuntimeError(_err())
-    n = L.orc_matrix_nrows(h)
+    nr = L.orc_matrix_nrows(h)
+    n = L.orc_matrix_ncols(h)
     nnz = L.orc_matrix_nnz(h)
     colptr = np.zeros(n + 1, dtype=np.int64)
     rowval = np.zeros(nnz, dtype=np.int64)
@@ -227,16 +235,17 @@ def _take_matrix(h):
     L.orc_matrix_copy(h, _p(colptr), _p(rowval), _p(nzval))
     dropped = L.orc_matrix_zeros_dropped(h)
     L.orc_matrix_free(h)
-    K = sp.csc_matrix((nzval, rowval - 1, colptr - 1), shape=(n, n))
+    K = sp.csc_matrix((nzval, rowval - 1, colptr - 1), shape=(nr, n))
     return K, int(dropped)
 
 
 class Assembler:
-    """SysmatAssemblerSparse / SysmatAssemblerSparseSymm restated."""
+    """SysmatAssemblerSparse / SysmatAssemblerSparseSymm / SysmatAssemblerSparseDiag
+    / SysmatAssemblerSparseHRZLumpingSymm restated (kind overrides symmetric)."""
 
-    def __init__(self, symmetric, nrows, ncols):
-        self.h = lib().orc_assembler_create(ASM_SPARSE_SYMM if symmetric else ASM_SPARSE,
-                                            nrows, ncols)
+    def __init__(self, symmetric, nrows, ncols, kind=None):
+        k = kind if kind is not None else (ASM_SPARSE_SYMM if symmetric else ASM_SPARSE)
+        self.h = lib().orc_assembler_create(k, nrows, ncols)
         if not self.h:
             raise ValueError(_err())
         self.zeros_dropped = 0
@@ -287,7 +296,7 @@ def _coef(kind, data, keep):
 
 
 def bilform(form, etype, conn, xyz, dofnums, nalldofs, pc, w, coef, coef_kind=COEF_CONST,
-            otherdim=1.0, m=3, symmetric=True, phases=False):
+            otherdim=1.0, m=3, symmetric=True, phases=False, asm=None):
     """One bilinear form, assembled like the reference's 4/5-argument call.
 
     Returns the scipy CSC matrix (and, optionally, the number of exact zeros
@@ -297,11 +306,34 @@ def bilform(form, etype, conn, xyz, dofnums, nalldofs, pc, w, coef, coef_kind=CO
     P = _problem(etype, conn, xyz, dofnums, nalldofs, pc, w, otherdim, keep)
     Cf = _coef(coef_kind, coef, keep)
     ph = np.zeros(3)
-    h = lib().orc_bilform(C.byref(P), form, C.byref(Cf), m,
-                          ASM_SPARSE_SYMM if symmetric else ASM_SPARSE, _p(ph))
+    kind = asm if asm is not None else (ASM_SPARSE_SYMM if symmetric else ASM_SPARSE)
+    h = lib().orc_bilform(C.byref(P), form, C.byref(Cf), m, kind, _p(ph))
     K, dropped = _take_matrix(h)
     if phases:
         return K, dropped, ph
+    return K
+
+
+def bilform_convection(etype, conn, xyz, dofnums, nalldofs, pc, w, velocity, otherdim=1.0):
+    """bilform_convection (scalar field) with SysmatAssemblerSparse; velocity
+    nnodes x nsd."""
+    keep = []
+    P = _problem(etype, conn, xyz, dofnums, nalldofs, pc, w, otherdim, keep)
+    v = np.ascontiguousarray(velocity, dtype=np.float64)
+    h = lib().orc_bilform_convection(C.byref(P), _p(v), v.shape[1])
+    K, _ = _take_matrix(h)
+    return K
+
+
+def bilform_masslike(etype, conn, xyz, dofnums, nalldofs, pc, w, coef, coef_kind=COEF_CONST,
+                     otherdim=1.0, m=3):
+    """bilform_masslike with SysmatAssemblerSparse: the nelem*ndn x nalldofs
+    matrix whose rows (i-1)*ndn+1 .. i*ndn belong to element i; coef ndn x ndn
+    (constant, per element or per quadrature point)."""
+    keep = []
+    P = _problem(etype, conn, xyz, dofnums, nalldofs, pc, w, otherdim, keep)
+    Cf = _coef(coef_kind, coef, keep)
+    K, _ = _take_matrix(lib().orc_bilform_masslike(C.byref(P), C.byref(Cf), m))
     return K
 
 

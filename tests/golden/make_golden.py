@@ -103,6 +103,16 @@ def assembler_kats():
         "source": f"{rel}:{line}", "size": 7, "form": "mtm",
         "mats": [m1, m2], "dofs": [i1, i2], "expected": testA,
     }
+    txt, line = module_text(src, "mmassembly2ya2", rel)
+    m1 = matrices_after(txt, r"\bm1 = \[")[0]
+    m2 = matrices_after(txt, r"\bm2 = \[")[0]
+    i1 = int_list(re.search(r"i1 = vec\(\[([^\]]*)\]\)", txt).group(1))
+    i2 = int_list(re.search(r"i2 = vec\(\[([^\]]*)\]\)", txt).group(1))
+    testA = matrices_after(txt, r"testA = \[")[0]
+    kats["sparse_diag_mtm"] = {
+        "source": f"{rel}:{line}", "kind": "diag", "size": 7, "form": "mtm",
+        "mats": [m1, m2], "dofs": [i1, i2], "expected": testA,
+    }
     txt, line = module_text(src, "massnomat1", rel)
     ms = matrices_after(txt, r"\bm = \[")
     asm = re.findall(r"assemble!\(a, m, \[([^\]]*)\], \[([^\]]*)\]\)", txt)
@@ -233,11 +243,25 @@ def cg_case():
     return {"source": f"{rel}:{line}", "A": A, "b": [r[0] for r in b], "maxiter": maxiter}
 
 
+def masslike_case():
+    """bilform_masslike known answer (test/test_forms.jl, module
+    mbilform_masslike_1): the L2 mesh's node coordinates, the Gauss order and
+    the expected dense matrix."""
+    rel = "test/test_forms.jl"
+    txt, line = module_text(read(rel), "mbilform_masslike_1", rel)
+    vec = lambda name: [float(x) for x in re.search(name + r"\s*=\s*\[([^\]]*)\]", txt)
+                        .group(1).split(",")]
+    order = int(re.search(r"GaussRule\(1,\s*(\d+)\)", txt).group(1))
+    G, _ = parse_matrix(txt, txt.index("[", re.search(r"Matrix\(G\)\s*==", txt).end()))
+    return {"source": f"{rel}:{line}", "xs": vec("xs"), "ys": vec("ys"), "gauss_order": order,
+            "G": G}
+
+
 def main():
     if not os.path.isdir(REF):
         sys.exit(f"reference sources not found at {REF}")
     data = {"assembler": assembler_kats(), "patch": patch_tests(), **coloring_and_pattern(),
-            "conjugategradient": cg_case()}
+            "conjugategradient": cg_case(), "masslike": masslike_case()}
     with open(OUT, "w") as f:
         json.dump(data, f, indent=1)
     print("wrote", OUT)

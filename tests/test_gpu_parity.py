@@ -149,6 +149,66 @@ def test_elasticity_fp64(ft, O, et, n, rule, coef):
     compare(Ks, _oracle_form(O, femm, O.LIN_ELASTIC, geom, u, oc, kind), structure=False)
 
 
+# ---------------------------------------------------------------- convection
+@pytest.mark.parametrize("et", ["H8", "T10", "H20", "Q4"])
+def test_convection_fp64(ft, O, et):
+    """bilform_convection (src/FEMMBaseModule.jl:1583-1625) with its default
+    SysmatAssemblerSparse, a nonuniform nodal velocity."""
+    rng = np.random.default_rng(21)
+    if et == "Q4":
+        fens, fes = ft.Q4block(1.0, 0.6, 5, 3)
+        fens.xyz = ft.meshes.jitter_interior(fens.xyz, (5, 3), 0.15, 7, box=(1.0, 0.6))
+        femm = ft.FEMMBase(ft.IntegDomain(fes, ft.GaussRule(2, 2), 0.3))
+    else:
+        gen = {"H8": ft.H8block, "H20": ft.H20block, "T10": ft.T10block}[et]
+        fens, fes = gen(1.0, 0.7, 1.3, 3, 2, 2)
+        fens.xyz = ft.meshes.jitter_interior(fens.xyz, (3, 2, 2), 0.15, 7, box=(1.0, 0.7, 1.3))
+        if et in ("H20", "T10"):
+            fens = ft.meshes.recompute_midpoints(fens, fes, 0)
+        r = ft.TetRule(4) if et == "T10" else ft.GaussRule(3, 3 if et == "H20" else 2)
+        femm = ft.FEMMBase(ft.IntegDomain(fes, r))
+    geom = ft.NodalField(fens.xyz)
+    sd = fens.xyz.shape[1]
+    vel = ft.NodalField(rng.uniform(-1, 1, (fens.count(), sd)) + np.arange(1, sd + 1))
+    Q = _field(ft, fens.count(), 1)
+    K = ft.bilform_convection(femm, geom, vel, Q, ft.DataCache(1.2))
+    npts, Ns, dN, w, pc = femm.integdomain.integrationdata()
+    Kr = O.bilform_convection(fes.code, fes.conn, geom.values, Q.dofnums, Q.nalldofs(), pc, w,
+                              vel.values, otherdim=femm.integdomain.otherdimension)
+    compare(K, Kr)
+
+
+# ---------------------------------------------------------------- div_grad
+@pytest.mark.parametrize("et,n,rule", [("H8", 3, ("G", 3, 2)), ("T10", 2, ("T", 4)),
+                                       ("H20", 2, ("G", 3, 3))])
+@pytest.mark.parametrize("coef", ["const", "per_element"])
+def test_div_grad_fp64(ft, O, et, n, rule, coef):
+    """bilform_div_grad (src/FEMMBaseModule.jl:1672-1723) with its default
+    SysmatAssemblerSparse; mixed precision within 1e-6 of FP64."""
+    gen = {"H8": ft.H8block, "H20": ft.H20block, "T10": ft.T10block}[et]
+    fens, fes = gen(1.0, 0.7, 1.3, n, n, n)
+    fens.xyz = ft.meshes.jitter_interior(fens.xyz, (n, n, n), 0.15, 6, box=(1.0, 0.7, 1.3))
+    if et in ("H20", "T10"):
+        fens = ft.meshes.recompute_midpoints(fens, fes, 0)
+    r = ft.GaussRule(*rule[1:]) if rule[0] == "G" else ft.TetRule(rule[1])
+    femm = ft.FEMMBase(ft.IntegDomain(fes, r))
+    geom = ft.NodalField(fens.xyz)
+    u = _field(ft, fens.count(), 3)
+    rng = np.random.default_rng(12)
+    if coef == "const":
+        cf, oc, kind = ft.DataCache(1.8e-3), np.array([1.8e-3]), 0
+    else:
+        mu = rng.lognormal(np.log(1e-3), 0.5, fes.count())
+        cf, oc, kind = ft.ElementwiseData(mu), mu.reshape(-1, 1), 1
+    K = ft.bilform_div_grad(femm, geom, u, cf)
+    Kr = _oracle_form(O, femm, O.DIV_GRAD, geom, u, oc, kind, symmetric=False)
+    compare(K, Kr)
+    Km = ft.bilform_div_grad(femm, ft.SysmatAssemblerGPU(symmetric=False, precision="mixed"),
+                             geom, u, cf)
+    x = rng.uniform(-1, 1, K.shape[0])
+    assert np.linalg.norm((Km - K) @ x) <= MIXED_TOL * np.linalg.norm(K @ x)
+
+
 # ---------------------------------------------------------------- dot / linform
 @pytest.mark.parametrize("et,ndn", [("H8", 1), ("H8", 3), ("T10", 3), ("H20", 1)])
 def test_dot_volume(ft, O, et, ndn):
@@ -171,6 +231,20 @@ def test_dot_volume(ft, O, et, ndn):
     v = np.ones(G.shape[0])
     V = 12.0 * 1.1 * 0.32
     assert abs(v @ G @ v - ndn * V) / V <= 1e-5
+
+
+def test_dot_unsymmetric_coefficient(ft, O):
+    """An unsymmetric ndn x ndn coefficient with SysmatAssemblerSparse gives an
+    unsymmetric matrix: the CSC export must read the values by columns."""
+    fens, fes = ft.H8block(1.0, 0.8, 0.6, 3, 2, 2)
+    femm = ft.FEMMBase(ft.IntegDomain(fes, ft.GaussRule(3, 2)))
+    geom = ft.NodalField(fens.xyz)
+    u = _field(ft, fens.count(), 3)
+    c = np.array([[2.0, 0.3, -0.1], [0.7, 1.5, 0.2], [0.05, -0.4, 1.1]])
+    K = ft.bilform_dot(femm, ft.SysmatAssemblerGPU(symmetric=False), geom, u, ft.DataCache(c))
+    Kr = _oracle_form(O, femm, O.DOT, geom, u, c, symmetric=False)
+    compare(K, Kr)
+    assert abs(K - K.T).max() > 0.0
 
 
 def test_dot_surface_q4_thickness(ft, O):
@@ -240,6 +314,46 @@ def test_general_dof_numbering_with_ebcs(ft, O):
                                ft.DeforModelRed3D, ft.DataCache(D))
     Kr = _oracle_form(O, femm, O.LIN_ELASTIC, geom, u, D, symmetric=False)
     compare(K, Kr)
+
+
+@pytest.mark.parametrize("form", ["elastic", "convection"])
+def test_blocked_extraction(ft, form):
+    """matrix_blocked_ff / fd / df / dd (src/MatrixUtilityModule.jl:675-806) of a
+    device matrix with the free DOFs numbered first equal the corresponding
+    slices of the full CSC export (symmetric and unsymmetric values)."""
+    fens, fes = ft.H8block(1.0, 0.8, 0.6, 3, 3, 2)
+    femm = ft.FEMMBase(ft.IntegDomain(fes, ft.GaussRule(3, 2)))
+    geom = ft.NodalField(fens.xyz)
+    on_face = np.flatnonzero(np.abs(fens.xyz[:, 0]) < 1e-12) + 1
+    asm = ft.SysmatAssemblerGPU(symmetric=False, result="device")
+    if form == "elastic":
+        u = ft.NodalField(np.zeros((fens.count(), 3)))
+        ft.setebc(u, on_face, True, [1, 2], 0.0)
+        ft.numberdofs(u)
+        K = ft.bilform_lin_elastic(femm, asm, geom, u, ft.DeforModelRed3D,
+                                   ft.DataCache(ft.isotropic_D(1.0, 0.3)))
+    else:
+        u = ft.NodalField(np.zeros((fens.count(), 1)))
+        ft.setebc(u, on_face, True, [1], 0.0)
+        ft.numberdofs(u)
+        vel = ft.NodalField(np.tile([1.0, 0.5, -0.2], (fens.count(), 1)))
+        K = ft.bilform_convection(femm, asm, geom, vel, u, ft.DataCache(1.0))
+    nf = u.nfreedofs()
+    full = K.to_scipy(drop_zeros=False).tocsc()
+    n = full.shape[0]
+    for fn, rows, cols in ((ft.matrix_blocked_ff, slice(0, nf), slice(0, nf)),
+                           (ft.matrix_blocked_fd, slice(0, nf), slice(nf, n)),
+                           (ft.matrix_blocked_df, slice(nf, n), slice(0, nf)),
+                           (ft.matrix_blocked_dd, slice(nf, n), slice(nf, n))):
+        B = fn(K, nf)
+        R = full[rows, cols].tocsc()
+        R.sort_indices()
+        B.sort_indices()
+        assert B.shape == R.shape
+        assert np.array_equal(B.indptr, R.indptr) and np.array_equal(B.indices, R.indices)
+        assert np.array_equal(B.data, R.data)
+    if form == "convection":
+        assert abs(full - full.T).max() > 0
 
 
 def test_permuted_node_numbering(ft, O):
@@ -345,6 +459,75 @@ def test_generic_assembler_kats(ft, kats):
     assert np.abs(A - A.T).max() == 0.0
 
 
+def test_generic_lumping_assemblers(ft, kats):
+    """SysmatAssemblerSparseDiag (test/test_basics.jl:135) and the HRZ recipe
+    (test/test_basics.jl:923-960) through the device assembler."""
+    k = kats["assembler"]["sparse_diag_mtm"]
+    a = ft.SysmatAssemblerSparseDiagGPU()
+    a.startassembly(5, 5, 3, 7, 7)
+    for m, d in zip(k["mats"], k["dofs"]):
+        m = np.array(m)
+        a.assemble(m.T @ m, d, d)
+    A = a.makematrix().toarray()
+    assert np.abs(np.diag(np.diag(np.array(k["expected"]))) - A).max() < 1e-5
+    rng = np.random.default_rng(5)
+    N, el = 30, rng.random((8, 8))
+    el = el + el.T
+    a = ft.SysmatAssemblerSparseHRZLumpingSymmGPU()
+    a.startassembly(8, 8, 3, N, N)
+    ref = np.zeros(N)
+    for d in ([10, 29, 15, 1, 7, 3, 6, 2], [15, 1, 7, 11, 29, 3, 8, 4],
+              [25, 1, 17, 13, 30, 13, 18, 14]):
+        a.assemble(el, d, d)
+        f = el.sum(axis=0).sum() / np.trace(el)
+        for i, dd in enumerate(d):
+            ref[dd - 1] += f * el[i, i]
+    M = a.makematrix()
+    assert np.abs(M.diagonal() - ref).sum() / np.linalg.norm(el) <= 1e-9
+
+
+@pytest.mark.parametrize("et,ndn,coef", [("H8", 3, "const"), ("T10", 3, "per_element"),
+                                         ("H20", 1, "const"), ("Q4", 3, "const")])
+@pytest.mark.parametrize("lumping", ["diag", "hrz"])
+def test_lumped_mass(ft, O, et, ndn, coef, lumping):
+    """bilform_dot with the lumping assemblers on the device against the
+    oracle's restatement of the same assembly."""
+    rng = np.random.default_rng(14)
+    if et == "Q4":
+        fens, fes = ft.Q4block(2.0, 1.5, 5, 4)
+        xyz = np.hstack([fens.xyz, rng.uniform(-0.05, 0.05, (fens.count(), 1))])
+        femm = ft.FEMMBase(ft.IntegDomain(fes, ft.GaussRule(2, 2), 0.01))
+    else:
+        gen = {"H8": ft.H8block, "H20": ft.H20block, "T10": ft.T10block}[et]
+        fens, fes = gen(1.0, 0.7, 1.3, 3, 2, 2)
+        xyz = ft.meshes.jitter_interior(fens.xyz, (3, 2, 2), 0.15, 4, box=(1.0, 0.7, 1.3))
+        if et in ("H20", "T10"):
+            fens.xyz = xyz
+            xyz = ft.meshes.recompute_midpoints(fens, fes, 0).xyz
+        r = ft.TetRule(4) if et == "T10" else ft.GaussRule(3, 3 if et == "H20" else 2)
+        femm = ft.FEMMBase(ft.IntegDomain(fes, r))
+    geom = ft.NodalField(xyz)
+    u = _field(ft, fens.count(), ndn)
+    if coef == "const":
+        c = np.eye(ndn) * 7.8e3
+        if ndn == 3:
+            c[0, 1] = c[1, 0] = 40.0
+        cf, oc, kind = ft.DataCache(c), c, 0
+    else:
+        rho = rng.uniform(1e3, 8e3, fes.count())
+        cf = ft.ElementwiseData(rho)
+        oc = np.stack([np.eye(ndn) * v for v in rho]).reshape(-1, ndn * ndn)
+        kind = 1
+    asm = (ft.SysmatAssemblerSparseDiagGPU() if lumping == "diag"
+           else ft.SysmatAssemblerSparseHRZLumpingSymmGPU())
+    M = ft.bilform_dot(femm, asm, geom, u, cf)
+    npts, Ns, dN, w, pc = femm.integdomain.integrationdata()
+    Mr = O.bilform(O.DOT, fes.code, fes.conn, geom.values, u.dofnums, u.nalldofs(), pc, w, oc,
+                   coef_kind=kind, otherdim=femm.integdomain.otherdimension, m=3,
+                   asm=O.ASM_DIAG if lumping == "diag" else O.ASM_HRZ)
+    compare(M, Mr)
+
+
 def test_generic_assembler_random(ft, O):
     """test/test_basics.jl:2100-2175: random symmetric matrices vs the oracle."""
     rng = np.random.default_rng(2)
@@ -391,3 +574,186 @@ def test_mixed_precision(ft, O, et):
     assert np.linalg.norm((K32 - K64) @ x) / np.linalg.norm(K64 @ x) <= MIXED_TOL
     assert abs(K32 - K64).max() / abs(K64).max() <= MIXED_TOL
     assert abs(K32 - K32.T).max() == 0.0
+
+
+# ---------------------------------------------------------------- masslike
+def _masslike_case(ft, et, seed=17):
+    rng = np.random.default_rng(seed)
+    if et == "Q4":
+        fens, fes = ft.Q4block(2.0, 1.5, 5, 4)
+        xyz = np.hstack([fens.xyz, rng.uniform(-0.05, 0.05, (fens.count(), 1))])
+        femm = ft.FEMMBase(ft.IntegDomain(fes, ft.GaussRule(2, 2), 0.01))
+    else:
+        gen = {"H8": ft.H8block, "H20": ft.H20block, "T10": ft.T10block, "T4": ft.T4block}[et]
+        fens, fes = gen(1.0, 0.7, 1.3, 3, 2, 2)
+        xyz = ft.meshes.jitter_interior(fens.xyz, (3, 2, 2), 0.15, 4, box=(1.0, 0.7, 1.3))
+        if et in ("H20", "T10"):
+            fens.xyz = xyz
+            xyz = ft.meshes.recompute_midpoints(fens, fes, 0).xyz
+        r = {"T10": ft.TetRule(4), "T4": ft.TetRule(1), "H20": ft.GaussRule(3, 3),
+             "H8": ft.GaussRule(3, 2)}[et]
+        femm = ft.FEMMBase(ft.IntegDomain(fes, r))
+    return rng, fens, fes, femm, ft.NodalField(xyz)
+
+
+@pytest.mark.parametrize("et,ndn,coef,m", [("H8", 1, "const", 3), ("T10", 3, "matrix", 3),
+                                           ("H20", 3, "per_element", 3), ("T4", 1, "per_qp", 3),
+                                           ("Q4", 3, "matrix", 3), ("Q4", 1, "const", 2)])
+def test_masslike(ft, O, et, ndn, coef, m):
+    """bilform_masslike (src/FEMMBaseModule.jl:1865-1917): the nelem*ndn x
+    nalldofs matrix through SysmatAssemblerSparse semantics (every element
+    block entry stored, explicit zeros included) against the oracle."""
+    rng, fens, fes, femm, geom = _masslike_case(ft, et)
+    u = _field(ft, fens.count(), ndn)
+    npts = femm.integdomain.integrationdata()[0]
+    if coef == "const":
+        cf, oc, kind = ft.DataCache(np.eye(ndn) * 2.5), np.eye(ndn) * 2.5, 0
+    elif coef == "matrix":
+        c = rng.uniform(0.5, 1.5, (ndn, ndn))
+        cf, oc, kind = ft.DataCache(c), c, 0
+    elif coef == "per_element":
+        rho = rng.uniform(1e3, 8e3, fes.count())
+        cf = ft.ElementwiseData(rho)
+        oc, kind = np.stack([np.eye(ndn) * v for v in rho]).reshape(-1, ndn * ndn), 1
+    else:
+        vals = rng.uniform(1.0, 2.0, (fes.count(), npts))
+        cf = ft.DataCache(np.eye(ndn), lambda cache, XYZ, tangents, feid, qpid:
+                          np.eye(ndn) * vals[feid - 1, qpid - 1])
+        oc = np.stack([[np.eye(ndn) * v for v in row] for row in vals]).reshape(
+            fes.count(), npts, ndn * ndn)
+        kind = 2
+    M = ft.bilform_masslike(femm, geom, u, cf, m=m)
+    _, Ns, dN, w, pc = femm.integdomain.integrationdata()
+    Mr = O.bilform_masslike(fes.code, fes.conn, geom.values, u.dofnums, u.nalldofs(), pc, w, oc,
+                            coef_kind=kind, otherdim=femm.integdomain.otherdimension, m=m)
+    assert M.shape == (fes.count() * ndn, u.nalldofs()) == Mr.shape
+    assert M.nnz == Mr.nnz == fes.count() * ndn * fes.nne * ndn
+    compare(M, Mr)
+    # each element row integrates its basis functions (partition of unity):
+    # the row sums of the scalar case are the element measures times c
+    if ndn == 1 and coef == "const":
+        assert np.all(np.asarray(M.sum(axis=1)).ravel() > 0)
+
+
+def test_masslike_errors(ft):
+    _, fens, fes, femm, geom = _masslike_case(ft, "H8")
+    u = _field(ft, fens.count(), 1)
+    with pytest.raises(ValueError, match="rectangular"):
+        ft.bilform_masslike(femm, ft.SysmatAssemblerGPU(symmetric=True), geom, u,
+                            ft.DataCache(1.0))
+    with pytest.raises(ft.FegpuError, match="only acceptable"):
+        ft.bilform_masslike(femm, geom, u, ft.DataCache(1.0), m=2)
+
+
+# ---------------------------------------------------------------- FF block
+def test_ffblock_assembler(ft, O):
+    """SysmatAssemblerFFBlock (src/AssemblyModule.jl:1144-1236): the device
+    forms, the generic protocol and masslike return the free-free block of
+    what the wrapped assembler makes."""
+    fens, fes = ft.H8block(1.0, 0.8, 0.6, 3, 3, 2)
+    femm = ft.FEMMBase(ft.IntegDomain(fes, ft.GaussRule(3, 2)))
+    geom = ft.NodalField(fens.xyz)
+    on_face = np.flatnonzero(np.abs(fens.xyz[:, 0]) < 1e-12) + 1
+    u = ft.NodalField(np.zeros((fens.count(), 3)))
+    ft.setebc(u, on_face, True, [1, 2], 0.0)
+    ft.numberdofs(u)
+    nf = u.nfreedofs()
+    D = ft.DataCache(ft.isotropic_D(1.0, 0.3))
+    full = ft.bilform_lin_elastic(femm, ft.SysmatAssemblerGPU(symmetric=False), geom, u,
+                                  ft.DeforModelRed3D, D).tocsc()
+    B = ft.bilform_lin_elastic(femm, ft.SysmatAssemblerFFBlockGPU(nf), geom, u,
+                               ft.DeforModelRed3D, D)
+    R = full[:nf, :nf].tocsc()
+    assert B.shape == (nf, nf)
+    assert np.array_equal(B.indptr, R.indptr) and np.array_equal(B.indices, R.indices)
+    assert np.array_equal(B.data, R.data)
+    # symmetric wrapped assembler: exact zeros of S + S' are not stored
+    Bs = ft.bilform_lin_elastic(femm, ft.SysmatAssemblerFFBlockGPU(
+        ft.SysmatAssemblerGPU(symmetric=True), nf), geom, u, ft.DeforModelRed3D, D)
+    Rs = ft.bilform_lin_elastic(femm, ft.SysmatAssemblerGPU(symmetric=True), geom, u,
+                                ft.DeforModelRed3D, D).tocsc()[:nf, :nf]
+    Rs.eliminate_zeros()
+    assert Bs.nnz == Rs.nnz and abs(Bs - Rs).max() == 0.0
+    # the generic protocol
+    rng = np.random.default_rng(5)
+    a = ft.SysmatAssemblerFFBlockGPU(7, 5)
+    a.startassembly(4, 4, 10, 11, 9)
+    o = O.Assembler(False, 11, 9)
+    for _ in range(10):
+        Mk = rng.uniform(-1, 1, (4, 4))
+        r, c = rng.permutation(11)[:4] + 1, rng.permutation(9)[:4] + 1
+        a.assemble(Mk, r, c)
+        o.assemble(Mk, r, c)
+    A = a.makematrix()
+    Ar = o.make().tocsc()[:7, :5]
+    assert A.shape == (7, 5) and A.nnz == Ar.nnz and abs(A - Ar).max() == 0.0
+    # masslike through the block assembler
+    q = _field(ft, fens.count(), 1)
+    Mfull = ft.bilform_masslike(femm, geom, q, ft.DataCache(1.0))
+    Mb = ft.bilform_masslike(femm, ft.SysmatAssemblerFFBlockGPU(10, 30), geom, q,
+                             ft.DataCache(1.0))
+    assert Mb.shape == (10, 30) and abs(Mb - Mfull.tocsc()[:10, :30]).max() == 0.0
+
+
+def test_generic_assembler_rectangular(ft, O):
+    """SysmatAssemblerSparse with rows != columns and repeated DOFs (sums in
+    input order) through the device makematrix! and CSC export."""
+    rng = np.random.default_rng(8)
+    a = ft.SysmatAssemblerGPU(symmetric=False)
+    a.startassembly(3, 5, 300, 41, 67)
+    o = O.Assembler(False, 41, 67)
+    for _ in range(300):
+        Mk = rng.uniform(-1, 1, (3, 5))
+        r = rng.integers(1, 42, 3)
+        c = rng.integers(1, 68, 5)
+        a.assemble(Mk, r, c)
+        o.assemble(Mk, r, c)
+    A = a.makematrix()
+    Ar = o.make()
+    assert A.shape == Ar.shape == (41, 67)
+    A, Ar = A.tocsc(), Ar.tocsc()
+    assert np.array_equal(A.indptr, Ar.indptr) and np.array_equal(A.indices, Ar.indices)
+    assert np.array_equal(A.data, Ar.data)
+
+
+def test_async_export_pipeline(ft):
+    """fegpu_matrix_copy_values_async: two matrices of one dofmap assembled in
+    turn while the other's values travel to the host; a form that writes a
+    matrix waits for its copy in flight, so every exported buffer holds the
+    values of its own assembly."""
+    import ctypes as C
+    import torch
+    nat = ft._native
+    L = nat.load()
+    fens, fes = ft.H8block(1.0, 0.8, 0.6, 6, 5, 4)
+    femm = ft.FEMMBase(ft.IntegDomain(fes, ft.GaussRule(3, 2)))
+    geom = ft.NodalField(fens.xyz)
+    u = _field(ft, fens.count(), 3)
+    asm = ft.SysmatAssemblerGPU(result="device")
+    K = ft.bilform_lin_elastic(femm, asm, geom, u, ft.DeforModelRed3D,
+                               ft.DataCache(ft.isotropic_D(1.0, 0.3)))
+    nnz = K.dm.nnz
+    k2 = C.c_void_p()
+    nat.check(L.fegpu_matrix_create(K.dm.h, C.byref(k2)))
+    mats = [K.h, k2.value]
+    bufs = [torch.empty(nnz, dtype=torch.float64, pin_memory=True).numpy() for _ in range(4)]
+    scales = [1.0, 2.0, 3.0, 4.0]
+    try:
+        for i, sc in enumerate(scales):
+            D = np.ascontiguousarray(ft.isotropic_D(sc, 0.3).ravel())
+            cf = nat.Coef(nat.COEF_CONST, 36, D.ctypes.data)
+            nat.check(L.fegpu_bilform_lin_elastic(mats[i & 1], C.byref(cf), nat.FP64))
+            nat.check(L.fegpu_matrix_copy_values_async(mats[i & 1], bufs[i].ctypes.data))
+        for h in mats:
+            nat.check(L.fegpu_matrix_wait_export(h))
+        last2 = np.empty(nnz)
+        nat.check(L.fegpu_matrix_copy_values(k2.value, nat.ptr(last2)))
+    finally:
+        nat.check(L.fegpu_matrix_destroy(k2.value))
+    # each buffer holds exactly the values of its own assembly
+    assert np.array_equal(K.values(), bufs[2]) and np.array_equal(last2, bufs[3])
+    # the elasticity matrix is linear in E: buffer i = scale_i x buffer 0 (to
+    # rounding; entries formed by cancellation get an absolute bound)
+    top = np.abs(bufs[0]).max()
+    for i, sc in enumerate(scales):
+        assert np.allclose(bufs[i], sc * bufs[0], rtol=1e-12, atol=1e-13 * sc * top)

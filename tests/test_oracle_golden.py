@@ -51,6 +51,37 @@ def test_kat_sparse_and_symm_agree(O, kats):
     assert np.abs(ref - out[1]).max() < 1e-5
 
 
+def test_kat_sparse_diag(O, kats):
+    # test/test_basics.jl:135 (mmassembly2ya2): SysmatAssemblerSparseDiag keeps
+    # the element diagonals: the diagonal of the full assembly
+    k = kats["assembler"]["sparse_diag_mtm"]
+    ref = np.array(k["expected"])
+    a = O.Assembler(True, 7, 7, kind=O.ASM_DIAG)
+    for m, d in zip(k["mats"], k["dofs"]):
+        m = np.array(m)
+        a.assemble(m.T @ m, d, d)
+    A = _dense(a.make())
+    assert np.abs(np.diag(np.diag(ref)) - A).max() < 1e-5
+
+
+def test_hrz_lumping_recipe(O):
+    # test/test_basics.jl:923-960 (mmhrzass1): the HRZ diagonal against its
+    # definition, on the test's DOF lists (seeded matrix instead of rand)
+    rng = np.random.default_rng(5)
+    N, el = 30, rng.random((8, 8))
+    el = el + el.T
+    a = O.Assembler(True, N, N, kind=O.ASM_HRZ)
+    ref = np.zeros(N)
+    for d in ([10, 29, 15, 1, 7, 3, 6, 2], [15, 1, 7, 11, 29, 3, 8, 4],
+              [25, 1, 17, 13, 30, 13, 18, 14]):
+        a.assemble(el, d, d)
+        f = el.sum(axis=0).sum() / np.trace(el)
+        for i, dd in enumerate(d):
+            ref[dd - 1] += f * el[i, i]
+    M = a.make()
+    assert np.abs(M.diagonal() - ref).sum() / np.linalg.norm(el) <= 1e-9
+
+
 def test_kat_spot_values(O, kats):
     # test/test_basics.jl:1577 (massnomat1): entries after the deferred makematrix!
     k = kats["assembler"]["nomatrixresult"]
@@ -231,3 +262,20 @@ def test_conjugategradient_on_reference_system(O, kats):
     x = O.conjugategradient(A, b, np.zeros(len(b)), c["maxiter"])
     assert np.linalg.norm(A @ x - b) <= 1e-12 * np.linalg.norm(b)
     assert np.allclose(x, np.linalg.solve(A, b), rtol=1e-10, atol=1e-12)
+
+
+def test_kat_masslike(O, kats):
+    """bilform_masslike on the reference's two-element line mesh: each element
+    owns one row; the row holds the integrals of the element's basis functions
+    (exact equality, as the reference asserts)."""
+    c = kats["masslike"]
+    xyz = np.stack([c["xs"], c["ys"]], axis=1)
+    conn = np.array([[i + 1, i + 2] for i in range(len(c["xs"]) - 1)], dtype=np.int64)
+    dofnums = np.arange(1, len(c["xs"]) + 1, dtype=np.int64).reshape(-1, 1)
+    pc, w = O.gauss_rule(1, c["gauss_order"])
+    G = O.bilform_masslike(O.L2, conn, xyz, dofnums, len(c["xs"]), pc, w, np.eye(1))
+    assert G.shape == (len(conn), len(c["xs"]))
+    assert np.array_equal(G.toarray(), np.array(c["G"]))
+    # SysmatAssemblerSparse keeps the explicit structure: one entry per
+    # (element row, element DOF)
+    assert G.nnz == conn.size
