@@ -311,6 +311,11 @@ void run_gather(fegpu_dofmap *dm, int form, KArgs &a) {
     if (v > 0.0 && v <= 1.0) share = v;
   }
   const int block_sms = std::max(1, static_cast<int>(ctx->num_sms * share));
+  if (!ctx->tc_status.p) {
+    ctx->tc_status.alloc(sizeof(int));
+    FEGPU_CUDA(cudaMemsetAsync(ctx->tc_status.p, 0, sizeof(int), s0));
+  }
+  a.status = ctx->tc_status.as<int>();
   if (ctx->timing) FEGPU_CUDA(cudaEventRecord(ctx->ev0, s0));
   FEGPU_CUDA(cudaEventRecord(ctx->ev_gather[0], s0));  // work before this call
   FEGPU_CUDA(cudaStreamWaitEvent(ctx->side, ctx->ev_gather[0], 0));
@@ -337,6 +342,14 @@ void run_gather(fegpu_dofmap *dm, int form, KArgs &a) {
     float ms = 0.f;
     FEGPU_CUDA(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
     ctx->kernel_ms += ms;
+  }
+  // the tensor-core element kernel reports a wait that ran out
+  int st = 0;
+  FEGPU_CUDA(cudaMemcpyAsync(&st, ctx->tc_status.p, sizeof(int), cudaMemcpyDeviceToHost, s0));
+  FEGPU_CUDA(cudaStreamSynchronize(s0));
+  if (st != 0) {
+    FEGPU_CUDA(cudaMemsetAsync(ctx->tc_status.p, 0, sizeof(int), s0));
+    throw Error{FEGPU_ERR_DEVICE, "mixed path: tensor-core completion wait ran out"};
   }
 }
 

@@ -97,6 +97,8 @@ struct fegpu_context {
   std::vector<cudaEvent_t> ev_blocks, ev_gather;
   // copies of finished matrices to host memory (fegpu_matrix_copy_values_async)
   cudaStream_t export_stream = nullptr;
+  // status word of the tensor-core element kernel (0 = ok), made on first use
+  fegpu::DevBuf tc_status;
 };
 
 struct fegpu_femm {

@@ -3,8 +3,11 @@
 // build compiles them in parallel.
 #pragma once
 
+#include <cstdlib>
+
 #include "elements.cuh"
 #include "mixed_fast.cuh"
+#include "mixed_tc.cuh"
 
 namespace fegpu {
 
@@ -44,7 +47,10 @@ int launch_mixed_et(int form, const KArgs &a, int sms, cudaStream_t s) {
     case F_DIFF_ISO: return launch_blocks_mixed_t<ET, F_DIFF_ISO, 1>(a, sms, s);
     case F_DIFF_GEN: return launch_blocks_mixed_t<ET, F_DIFF_GEN, 1>(a, sms, s);
     case F_ELAST_ISO:
-      if constexpr (SOLID) return launch_blocks_mixed_t<ET, F_ELAST_ISO, 3>(a, sms, s);
+      if constexpr (SOLID) {
+        if (tc_enabled(a)) return launch_blocks_tc<ET>(a, sms, s);
+        return launch_blocks_mixed_t<ET, F_ELAST_ISO, 3>(a, sms, s);
+      }
       break;
     case F_ELAST_GEN:
       if constexpr (SOLID) return launch_blocks_mixed_t<ET, F_ELAST_GEN, 3>(a, sms, s);

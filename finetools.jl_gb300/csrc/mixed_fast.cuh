@@ -86,34 +86,24 @@ inline int max_fast_tile(int etype) {
 }
 inline int default_fast_tile(int etype) { return max_fast_tile(etype); }
 
-template <int ET, int FORM, int NDN>
-__device__ __forceinline__ void mixed_tile_fast(const KArgs &a, int64_t eb, int ne,
-                                                unsigned char *smem, float *ke, int64_t e0) {
+// Phases A, B and B' of the tile (shared with the tensor-core tile of
+// mixed_tc.cuh): connectivity and Lame pairs, FP32 coordinates relative to the
+// element's first node, J / det J / J^-1 per (element, point), the FP64
+// geometry of distorted elements and the point weights.  Starts and ends with
+// a CTA barrier.
+template <int ET, int FORM>
+__device__ __forceinline__ void fast_geometry(const KArgs &a, int64_t eb, int ne, int32_t *sConn,
+                                              float4 *fX, float *sJinv, float *sDet, float *sW,
+                                              float *sLame) {
   constexpr int NNE = ElemT<ET>::NNE, MDIM = ElemT<ET>::MDIM;
-  constexpr int NBLK = NNE * (NNE + 1) / 2;
-  constexpr int BS = NDN * NDN;
   constexpr bool GRAD = FORM != F_DOT;
-  constexpr int SLOTS = fast_stride(NNE);
-  using T = FastTiles<NNE>;
-  constexpr int TA = T::TA, TB = T::TB, NT = T::NT;
-  static_assert(FORM == F_DIFF_ISO || FORM == F_ELAST_ISO || FORM == F_DOT, "isotropic forms");
-  const int npts = a.npts, te = a.te;
-  const FastLayout L = fast_layout(NNE, npts, te, NDN);
-  const float *fN = a.tab32;
+  const int npts = a.npts;
   const float *fdN = a.tab32 + npts * NNE;
   const float *fw = fdN + npts * NNE * MDIM;
-  int32_t *sConn = reinterpret_cast<int32_t *>(smem + L.conn);
-  float4 *fX = reinterpret_cast<float4 *>(smem + L.fx);
-  float *sJinv = reinterpret_cast<float *>(smem + L.jinv);
-  float *sDet = reinterpret_cast<float *>(smem + L.det);
-  float *sW = reinterpret_cast<float *>(smem + L.w);
-  float *sLame = reinterpret_cast<float *>(smem + L.lame);
-  float4 *sG = reinterpret_cast<float4 *>(smem + L.g);
   const int tid = threadIdx.x, nth = blockDim.x;
   const double *tabdN = a.tab + npts * NNE;
   const float tol = static_cast<float>(a.distort_tol);
   const float odim = static_cast<float>(a.otherdim);
-
   __syncthreads();  // the previous tile is done with shared memory
   for (int i = tid; i < ne * NNE; i += nth) sConn[i] = a.conn[eb * NNE + i];
   if constexpr (FORM == F_ELAST_ISO) {
@@ -229,6 +219,33 @@ __device__ __forceinline__ void mixed_tile_fast(const KArgs &a, int64_t eb, int 
     sW[i] = w;
   }
   __syncthreads();
+}
+
+template <int ET, int FORM, int NDN>
+__device__ __forceinline__ void mixed_tile_fast(const KArgs &a, int64_t eb, int ne,
+                                                unsigned char *smem, float *ke, int64_t e0) {
+  constexpr int NNE = ElemT<ET>::NNE, MDIM = ElemT<ET>::MDIM;
+  constexpr int NBLK = NNE * (NNE + 1) / 2;
+  constexpr int BS = NDN * NDN;
+  constexpr bool GRAD = FORM != F_DOT;
+  constexpr int SLOTS = fast_stride(NNE);
+  using T = FastTiles<NNE>;
+  constexpr int TA = T::TA, TB = T::TB, NT = T::NT;
+  static_assert(FORM == F_DIFF_ISO || FORM == F_ELAST_ISO || FORM == F_DOT, "isotropic forms");
+  const int npts = a.npts, te = a.te;
+  const FastLayout L = fast_layout(NNE, npts, te, NDN);
+  const float *fN = a.tab32;
+  const float *fdN = a.tab32 + npts * NNE;
+  int32_t *sConn = reinterpret_cast<int32_t *>(smem + L.conn);
+  float4 *fX = reinterpret_cast<float4 *>(smem + L.fx);
+  float *sJinv = reinterpret_cast<float *>(smem + L.jinv);
+  float *sDet = reinterpret_cast<float *>(smem + L.det);
+  float *sW = reinterpret_cast<float *>(smem + L.w);
+  float *sLame = reinterpret_cast<float *>(smem + L.lame);
+  float4 *sG = reinterpret_cast<float4 *>(smem + L.g);
+  const int tid = threadIdx.x, nth = blockDim.x;
+
+  fast_geometry<ET, FORM>(a, eb, ne, sConn, fX, sJinv, sDet, sW, sLame);
   // C. (g, w) per (element, point, node): thread t handles node t % NNE of
   // the (element, point) rows t / NNE, t / NNE + R, ... (R = threads / NNE)
   if constexpr (GRAD) {

@@ -27,6 +27,8 @@ namespace fegpu {
 namespace {
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[FEGPU_NOALLOC_SCRATCH_BYTES];
+// status word of the tensor-core element kernel (0 = ok)
+static __device__ int g_noalloc_status;
 
 // Device address of the array, looked up once per device with that device
 // current (in host code the symbol is only a host-side stand-in).
@@ -41,6 +43,19 @@ void *scratch_address(int device) {
     addr[device] = p;
   }
   return addr[device];
+}
+
+int *status_address(int device) {
+  static std::mutex mu;
+  static void *addr[256] = {};
+  std::lock_guard<std::mutex> lock(mu);
+  FEGPU_REQUIRE(device >= 0 && device < 256, "device ordinal out of range");
+  if (!addr[device]) {
+    void *p = nullptr;
+    FEGPU_CUDA(cudaGetSymbolAddress(&p, g_noalloc_status));
+    addr[device] = p;
+  }
+  return static_cast<int *>(addr[device]);
 }
 
 size_t align256(size_t n) { return (n + 255) / 256 * 256; }
@@ -188,6 +203,7 @@ extern "C" int fegpu_bilform_lin_elastic_noalloc(fegpu_matrix *K, const fegpu_co
     g.val = K->val.as<double>();
     g.maxdeg = dm->maxdeg;
     await_export(K, s);
+    a.status = status_address(ctx->device);  // enables the tensor-core element blocks
     const int64_t nch = static_cast<int64_t>(dm->na_chunk_nodes.size()) - 1;
     for (int64_t c = 0; c < nch; ++c) {
       a.e0 = c * chunk;
@@ -199,6 +215,12 @@ extern "C" int fegpu_bilform_lin_elastic_noalloc(fegpu_matrix *K, const fegpu_co
       ctx->launches += launch_gather_inline_slot(fm->etype, 3, g, ctx->num_sms, s);
     }
     FEGPU_CUDA(cudaStreamSynchronize(s));
+    int st = 0;
+    FEGPU_CUDA(cudaMemcpy(&st, a.status, sizeof(int), cudaMemcpyDeviceToHost));
+    if (st != 0) {
+      FEGPU_CUDA(cudaMemset(a.status, 0, sizeof(int)));
+      throw Error{FEGPU_ERR_DEVICE, "mixed path: tensor-core completion wait ran out"};
+    }
     return FEGPU_OK;
   } catch (const Error &e) {
     set_error(e.msg);

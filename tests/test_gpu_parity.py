@@ -757,3 +757,44 @@ def test_async_export_pipeline(ft):
     top = np.abs(bufs[0]).max()
     for i, sc in enumerate(scales):
         assert np.allclose(bufs[i], sc * bufs[0], rtol=1e-12, atol=1e-13 * sc * top)
+
+
+@pytest.mark.parametrize("et", ["H20", "T10", "H8", "T4"])
+def test_mixed_tensor_core_blocks(ft, et, monkeypatch):
+    """The tensor-core element blocks (tcgen05 kind::tf32, split hi/lo
+    operands) against the FP64 path, beside the FP32-pipe blocks: both within
+    the mixed tolerance, exactly symmetric, and not the same arithmetic."""
+    rng = np.random.default_rng(9)
+    if et == "H20":
+        fens, fes, _ = ft.h20_elastic_mesh(n=4, distort_fraction=0.05)
+        r = ft.GaussRule(3, 3)
+    elif et == "T10":
+        fens, fes = ft.t10_elastic_mesh(n=3)
+        r = ft.TetRule(4)
+    elif et == "H8":
+        fens, fes = ft.H8block(1.0, 0.8, 0.6, 5, 4, 3)
+        fens.xyz = ft.meshes.jitter_interior(fens.xyz, (5, 4, 3), 0.2, 3, box=(1.0, 0.8, 0.6))
+        r = ft.GaussRule(3, 3)
+    else:
+        fens, fes = ft.T4block(1.0, 0.8, 0.6, 4, 3, 3)
+        fens.xyz = ft.meshes.jitter_interior(fens.xyz, (4, 3, 3), 0.2, 3, box=(1.0, 0.8, 0.6))
+        r = ft.TetRule(1)
+    femm = ft.FEMMBase(ft.IntegDomain(fes, r))
+    geom = ft.NodalField(fens.xyz)
+    u = _field(ft, fens.count(), 3)
+    E = rng.lognormal(np.log(70e9), 0.5, fes.count())
+    nu = rng.uniform(0.2, 0.35, fes.count())
+    cf = ft.IsotropicElementwise(E, nu)
+    K64 = ft.bilform_lin_elastic(femm, ft.SysmatAssemblerGPU(), geom, u, ft.DeforModelRed3D, cf)
+    out = {}
+    for flag in ("1", "0"):  # tensor-core blocks (opt-in) and the default FP32-pipe tile
+        monkeypatch.setenv("FEGPU_MIXED_TC", flag)
+        out[flag] = ft.bilform_lin_elastic(femm, ft.SysmatAssemblerGPU(precision="mixed"), geom,
+                                           u, ft.DeforModelRed3D, cf)
+    x = rng.uniform(-1, 1, K64.shape[0])
+    for flag, K in out.items():
+        err_kx = np.linalg.norm((K - K64) @ x) / np.linalg.norm(K64 @ x)
+        err_max = abs(K - K64).max() / abs(K64).max()
+        assert err_kx <= MIXED_TOL and err_max <= MIXED_TOL, (flag, err_kx, err_max)
+        assert abs(K - K.T).max() == 0.0
+    assert abs(out["1"] - out["0"]).max() > 0.0

@@ -11,6 +11,14 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
+@pytest.fixture(autouse=True)
+def _fp32_pipe_single_calls(monkeypatch):
+    """The persistent batch kernel forms element blocks on the FP32 pipe; the
+    single-call references of these tests use the same tile (the single-call
+    tensor-core blocks are checked against FP64 in test_gpu_parity)."""
+    monkeypatch.setenv("FEGPU_MIXED_TC", "0")
+
+
 def _field(ft, n, ndn):
     return ft.numberdofs(ft.NodalField(np.zeros((n, ndn))))
 
