@@ -47,6 +47,23 @@ def env_rank():
             int(os.environ.get("LOCAL_RANK", "0")))
 
 
+def max_over_ranks(torch, dist, value):
+    """The largest of every rank's value (a time): the job is as slow as its
+    slowest replica.  NCCL reduces a device tensor, gloo a host one."""
+    if dist is None:
+        return float(value)
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(value)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(units_per_rank, world, seconds):
+    """Whole-job throughput of weakly scaled replicas: every rank processed
+    units_per_rank in (at most) `seconds`."""
+    return world * units_per_rank / seconds
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled every 50 ms; entering
     waits (up to 3 s) for the first sample, so the region that follows is
@@ -266,11 +283,7 @@ def time_steps(torch, stream, fn, steps, warmup, flush=None, dist=None):
             ev[1].record(stream)
             torch.cuda.synchronize()
             ms += ev[0].elapsed_time(ev[1])
-    if dist is not None:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    return ms
+    return max_over_ranks(torch, dist, ms)
 
 
 def fp64_peak_tflops(torch):
@@ -352,7 +365,7 @@ def run_ours(args):
     launches_timed = launches // nsteps_counted * args.steps
     E, N, nnz, ndof = fes.count(), fens.count(), dm.nnz, dm.ndof
     ms_step = ms / args.steps
-    value = world * E / (ms_step * 1e-3)
+    value = job_throughput(E, world, ms_step * 1e-3)
     B = algorithmic_bytes(E, 10, N, nnz, ndof, 0)
     peak, peak_src = measured_peaks()
     achieved = B / (kernel_ms_step * 1e-3) / 1e9
@@ -397,12 +410,8 @@ def run_ours(args):
         for Kh in mats:
             lib.nat.check(lib.L.fegpu_matrix_wait_export(Kh))
         torch.cuda.synchronize()
-        e2e_s = time.perf_counter() - t0
-        if dist is not None:
-            t = torch.tensor([e2e_s], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_s = float(t.item())
-        return world * E * args.steps / e2e_s
+        e2e_s = max_over_ranks(torch, dist, time.perf_counter() - t0)
+        return job_throughput(E * args.steps, world, e2e_s)
 
     e2e_seq = e2e_run(False)
     e2e_value = e2e_run(True)
