@@ -415,9 +415,11 @@ def run_ours(args):
 
     e2e_seq = e2e_run(False)
     e2e_value = e2e_run(True)
-    # both host buffers hold the (identical) assembled values: a strided sample
-    e2e_check = bool(np.array_equal(vals_h[0][::97], vals_h[1][::97]) and
-                     np.any(vals_h[0][::97] != 0.0))
+    # every host buffer written by the pipelined loop holds the assembled
+    # values (a strided sample against the device copy)
+    ref = K.values()[::97]
+    e2e_check = all(bool(np.array_equal(vals_h[i][::97], ref))
+                    for i in range(min(2, args.steps + args.warmup)))
     lib.nat.check(lib.L.fegpu_matrix_destroy(k2.value))
     lib.stats(reset=True)
     del K, asm

@@ -74,9 +74,10 @@ int choose_tile(int etype, int form, int precision, int npts) {
   const bool grad = form <= F_ELAST_GEN;
   const int tsize = (precision == FEGPU_MIXED && grad) ? 4 : 8;
   // shared-memory budget per CTA: measured on T10 60^3 elasticity (FP64),
-  // 72 KB (32 elements per tile) runs 1.36x faster than 100 KB (44): finer
-  // tiles balance the pair-block rounds and the waves of a colour better
-  const size_t budget = (etype == FEGPU_H20) ? 200 * 1024 : 72 * 1024;
+  // 82 KB (36 elements per tile) runs 1.05x faster than 72 KB (32) and 1.5x
+  // faster than 100 KB (44): two CTAs per SM either way, but the larger
+  // carve-out leaves the scatter's loads less L1
+  const size_t budget = (etype == FEGPU_H20) ? 200 * 1024 : 82 * 1024;
   const SmemLayout one = smem_layout(nne, mdim, npts, 1, tsize, grad);
   const SmemLayout two = smem_layout(nne, mdim, npts, 2, tsize, grad);
   const size_t per = two.total - one.total;
@@ -240,14 +241,35 @@ void run_colours(fegpu_dofmap *dm, int form, int precision, KArgs &a) {
   if (ctx->timing) FEGPU_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
   const int te_max = a.te;
   const bool fixed = std::getenv("FEGPU_FP64_TILE") != nullptr;
+  // resident CTAs per SM of the colour kernels: two (registers), one when a
+  // tile's shared memory leaves no room for a second
+  const size_t smem_max = form_smem_bytes(fm->etype, form, precision, fm->npts, te_max);
+  const int64_t slots =
+      static_cast<int64_t>(ctx->num_sms) * (smem_max + 1024 <= 113 * 1024 ? 2 : 1);
   for (int c = 0; c < ncol; ++c) {
     a.e0 = fm->color_offsets[c];
     a.e1 = fm->color_offsets[c + 1];
-    // small colours: smaller tiles, so that every SM gets about two CTAs
-    // (H8 20^3 diffusion, 1,000-element colours: 0.24 ms at 12 per tile
-    // against 0.35 ms at 21)
-    const int64_t per = (a.e1 - a.e0 + 2 * ctx->num_sms - 1) / (2 * ctx->num_sms);
-    a.te = fixed ? te_max : static_cast<int>(std::max<int64_t>(4, std::min<int64_t>(te_max, per)));
+    // elements per tile: the time of a colour goes as (waves of tiles over
+    // the CTA slots) x (elements per tile), so pick the tile in
+    // [te_max / 2, te_max] (at least 4) that minimises that product, ties to
+    // the larger tile (T10 60^3, 32.4 k-element colours: 36 per tile, three
+    // full waves, against four waves at 32); small colours get small tiles
+    // (H8 20^3 diffusion, 1,000-element colours: 4 per tile, one wave)
+    const int64_t n = a.e1 - a.e0;
+    int best = te_max;
+    if (!fixed) {
+      int64_t best_cost = -1;
+      for (int te = std::max(1, std::min(4, te_max)); te <= te_max; ++te) {
+        if (te < te_max / 2 && (n + te - 1) / te > slots) continue;
+        const int64_t waves = ((n + te - 1) / te + slots - 1) / slots;
+        const int64_t cost = waves * te;
+        if (best_cost < 0 || cost < best_cost || (cost == best_cost && te > best)) {
+          best_cost = cost;
+          best = te;
+        }
+      }
+    }
+    a.te = best;
     ctx->launches += launch_form(fm->etype, form, precision, dm->ndn, a, ctx->num_sms, ctx->stream);
   }
   a.te = te_max;

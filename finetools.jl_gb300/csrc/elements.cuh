@@ -212,7 +212,12 @@ __device__ __forceinline__ C geometry_qp(const XT *X, const XT *dN, int sdim,
 // per-point scalar (sJw):
 //   diffusion (scalar c):  WG = ((c Jac) w) g            (add_mggt_ut_only!)
 //   diffusion (kappa):     WG = (Jac w) (kappa g)         (add_gkgt_ut_only!)
-//   elasticity:            WG = (Jac w) g                 (Gram of the gradients)
+//   elasticity (general D): WG = (Jac w) g               (Gram of the gradients)
+//   elasticity (lam, mu):  WG = (s (Jac w)) g, s = mu (1 if mu = 0): the Gram
+//                          sums come out scaled by mu, and sJw[e, 0] holds
+//                          lam / s for the form map
+//                          V = (lam/s) M' + M'^T + I tr M' (mu != 0),
+//                          V = lam M' (mu = 0)
 //   dot:                   sJw = Jac                      (factor formed per pair)
 //   linform:               sJw = Jac w
 template <int NNE, int MDIM, int FORM, typename T>
@@ -240,7 +245,21 @@ __device__ __forceinline__ void qp_weights(const KArgs &a, int64_t es, int q, in
         wg[k * MDIM + m] = mul(Jw, acc);
       }
     *jw = Jw;
-  } else if constexpr (FORM == F_ELAST_ISO || FORM == F_ELAST_GEN) {
+  } else if constexpr (FORM == F_ELAST_ISO) {
+    T lam, mu;
+    if (a.coef_kind == FEGPU_COEF_ISO_LAME) {
+      lam = T(a.coef[2 * es]);
+      mu = T(a.coef[2 * es + 1]);
+    } else {
+      lam = T(a.cconst[0]);
+      mu = T(a.cconst[1]);
+    }
+    const T sc = mu != T(0) ? mu : T(1);
+    const T Jw = sc * (Jac * T(wq));
+#pragma unroll
+    for (int k = 0; k < NNE * MDIM; ++k) wg[k] = Jw * g[k];
+    if (q == 0) *jw = lam / sc;
+  } else if constexpr (FORM == F_ELAST_GEN) {
     const T Jw = Jac * T(wq);
 #pragma unroll
     for (int k = 0; k < NNE * MDIM; ++k) wg[k] = Jw * g[k];
@@ -429,20 +448,16 @@ __global__ void __launch_bounds__(kFormThreads) k_form(const KArgs a) {
             for (int n = 0; n < 3; ++n) M[m][n] = fma(x[m], y[n], M[m][n]);
         }
         if constexpr (FORM == F_ELAST_ISO) {
-          T lam, mu;
-          if (a.coef_kind == FEGPU_COEF_ISO_LAME) {
-            lam = T(a.coef[2 * es]);
-            mu = T(a.coef[2 * es + 1]);
-          } else {
-            lam = T(a.cconst[0]);
-            mu = T(a.cconst[1]);
-          }
-          const T mtr = mu * (M[0][0] + M[1][1] + M[2][2]);
+          // M holds mu M (the weights carry mu); r = lam / mu
+          const bool fold =
+              (a.coef_kind == FEGPU_COEF_ISO_LAME ? a.coef[2 * es + 1] : a.cconst[1]) != 0.0;
+          const T r = sJw[e * npts];
+          const T mtr = fold ? (M[0][0] + M[1][1]) + M[2][2] : T(0);
 #pragma unroll
           for (int ii = 0; ii < 3; ++ii)
 #pragma unroll
             for (int jj = 0; jj < 3; ++jj) {
-              T v = fma(lam, M[ii][jj], mu * M[jj][ii]);
+              T v = fma(r, M[ii][jj], fold ? M[jj][ii] : T(0));
               if (ii == jj) v += mtr;
               V[ii][jj] = v;
             }
