@@ -35,8 +35,10 @@ __device__ __forceinline__ void two_sum_acc(float &h, float &l, float v) {
 // each, in the warp's shared region), blocks of the incident elements in
 // element order, then one FP64 store per CSR value of the node's rows.
 // L2ONLY reads the blocks with ld.global.cg (no L1 allocation): required when
-// the blocks were written earlier in the same launch by other CTAs.
-template <int NNE, int NDN, bool INLINE_SLOT, bool L2ONLY = false>
+// the blocks were written earlier in the same launch by other CTAs.  PIPE
+// loads element k + 1's block entries before accumulating element k (more
+// registers: the persistent batch kernel, capped at 128, keeps the plain loop).
+template <int NNE, int NDN, bool INLINE_SLOT, bool L2ONLY = false, bool PIPE = !L2ONLY>
 __device__ __forceinline__ void gather_node(const GArgs &g, int32_t A, float *hi, float *lo,
                                             int lane) {
   constexpr int NBLK = NNE * (NNE + 1) / 2;
@@ -60,6 +62,73 @@ __device__ __forceinline__ void gather_node(const GArgs &g, int32_t A, float *hi
     tj[s] = task - tb[s] * NDN;
     trow[s] = tb[s] * NNE - tb[s] * (tb[s] - 1) / 2 - tb[s];  // pair(b, x) = trow + x, x >= b
   }
+  if constexpr (PIPE) {
+  __syncwarp();
+  // incident elements in element order, 32 at a time: lane k holds the k-th
+  // element, its local node index and its ring slot; the block entries and
+  // columns of element k + 1 are loaded before element k is accumulated, so
+  // the L2 round trips of consecutive elements overlap
+  const int64_t qa = g.n2e_ptr[A], qz = g.n2e_ptr[A + 1];
+  for (int64_t qb = qa; qb < qz; qb += 32) {
+    const int cnt = static_cast<int>(min(static_cast<int64_t>(32), qz - qb));
+    int32_t my_e = 0, my_slot = 0;
+    int my_a = 0;
+    if (lane < cnt) {
+      my_e = g.n2e_elem[qb + lane];
+      my_a = g.n2e_loc[qb + lane];
+      if constexpr (INLINE_SLOT) {
+        const int32_t ch = static_cast<int32_t>(g.chunk);
+        const int32_t ce = my_e / ch;
+        my_slot = (ce % g.ring) * ch + (my_e - ce * ch);
+      } else {
+        my_slot = g.n2e_slot[qb + lane];
+      }
+    }
+    float vc[NSLOT][NDN], vn[NSLOT][NDN];
+    int cc[NSLOT], cn[NSLOT];
+    auto fetch = [&](int k, float (&v)[NSLOT][NDN], int (&col)[NSLOT]) {
+      const int32_t e = __shfl_sync(0xffffffffu, my_e, k);
+      const int a = __shfl_sync(0xffffffffu, my_a, k);
+      const int32_t slot = __shfl_sync(0xffffffffu, my_slot, k);
+      const float *kb = g.ke + static_cast<int64_t>(slot) * NBLK * BS;
+      const uint16_t *pe = g.pos + (static_cast<int64_t>(e) * NNE + a) * NNE;
+      const int rowa = a * NNE - a * (a - 1) / 2 - a;
+#pragma unroll
+      for (int s2 = 0; s2 < NSLOT; ++s2) {
+        col[s2] = 0;
+#pragma unroll
+        for (int i = 0; i < NDN; ++i) v[s2][i] = 0.f;
+        if (lane + 32 * s2 < NTASK) {
+          const int b = tb[s2], j = tj[s2];
+          const bool up = a <= b;  // block (a, b) stored; else (b, a), transposed
+          const float *blk = kb + (up ? rowa + b : trow[s2] + a) * BS + (up ? j : j * NDN);
+          const int step = up ? NDN : 1;
+          col[s2] = pe[b] * NDN + j;
+#pragma unroll
+          for (int i = 0; i < NDN; ++i) v[s2][i] = L2ONLY ? __ldcg(blk + i * step) : blk[i * step];
+        }
+      }
+    };
+    fetch(0, vc, cc);
+    for (int k = 0; k < cnt; ++k) {
+      if (k + 1 < cnt) fetch(k + 1, vn, cn);
+#pragma unroll
+      for (int s2 = 0; s2 < NSLOT; ++s2) {
+        if (lane + 32 * s2 >= NTASK) break;
+#pragma unroll
+        for (int i = 0; i < NDN; ++i)
+          two_sum_acc(hi[i * cmax + cc[s2]], lo[i * cmax + cc[s2]], vc[s2][i]);
+      }
+      __syncwarp();
+#pragma unroll
+      for (int s2 = 0; s2 < NSLOT; ++s2) {
+        cc[s2] = cn[s2];
+#pragma unroll
+        for (int i = 0; i < NDN; ++i) vc[s2][i] = vn[s2][i];
+      }
+    }
+  }
+  } else {
   __syncwarp();
   for (int64_t q = g.n2e_ptr[A]; q < g.n2e_ptr[A + 1]; ++q) {
     const int64_t e = g.n2e_elem[q];
@@ -90,6 +159,7 @@ __device__ __forceinline__ void gather_node(const GArgs &g, int32_t A, float *hi
       for (int i = 0; i < NDN; ++i) two_sum_acc(hi[i * cmax + col], lo[i * cmax + col], v[i]);
     }
     __syncwarp();
+  }
   }
 #pragma unroll
   for (int i = 0; i < NDN; ++i) {
