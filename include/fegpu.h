@@ -176,9 +176,11 @@ int fegpu_matrix_copy_csc(fegpu_matrix *K, int drop_zeros, int64_t *colptr,
                           int64_t *rowval, double *nzval);
 /* values only, in the structural pattern order (re-assembly on a fixed mesh) */
 int fegpu_matrix_copy_values(fegpu_matrix *K, double *nzval);
-/* The same copy without waiting for it: queued on the context's export
- * stream behind the work already queued for K, it overlaps what the caller
- * queues next (the next assembly into another matrix, a coordinate upload).
+/* The same copy without waiting for it (no reference counterpart: the
+ * reference's makematrix! hands back a host matrix at once): queued on the
+ * context's export stream behind the work already queued for K, it overlaps
+ * what the caller queues next (the next assembly into another matrix, a
+ * coordinate upload).
  * nzval should be page-locked host memory and stays in use until
  * fegpu_matrix_wait_export(K) returns.  A form that writes K again waits on
  * the device for the copy first, so two matrices of one dofmap used in turn
