@@ -243,6 +243,52 @@ def cg_case():
     return {"source": f"{rel}:{line}", "A": A, "b": [r[0] for r in b], "maxiter": maxiter}
 
 
+def div_grad_cases():
+    """bilform_div_grad identities (test/test_forms.jl, modules
+    mbilform_div_grad_1..3): a constant velocity has no energy, a linear one
+    the energy 2 mu V |sym grad u|^2, and for any field the energy equals the
+    elasticity energy with C = diag(2mu, 2mu, 2mu, mu, mu, mu)."""
+    rel = "test/test_forms.jl"
+    src = read(rel)
+    out = []
+    for mod, kind in (("mbilform_div_grad_1", "constant_field"),
+                      ("mbilform_div_grad_2", "linear_field"),
+                      ("mbilform_div_grad_3", "vs_elastic")):
+        txt, line = module_text(src, mod, rel)
+        W, L, t = num(txt, "W"), num(txt, "L"), num(txt, "t")
+        sizes = dict(zip(["nl", "nt", "nw"], tuple_vals(txt, "nl, nt, nw")))
+        args = block_args(txt, "H8block")
+        env = {"W": W, "L": L, "t": t, **sizes}
+        rec = {"source": f"{rel}:{line}", "module": mod, "kind": kind,
+               "block": [env[a] for a in args[:3]] + [int(env[a]) for a in args[3:6]],
+               "gauss_order": int(re.search(r"GaussRule\(3,\s*(\d+)\)", txt).group(1)),
+               "volume": W * L * t, "mu": num(txt, "mu"), "tol": 1.0e-5}
+        if "u_x, u_y, u_z" in txt:
+            rec["uxyz"] = tuple_vals(txt, "u_x, u_y, u_z")
+        if "a, b, c, d" in txt:
+            rec["abcd"] = tuple_vals(txt, "a, b, c, d")
+        out.append(rec)
+    return out
+
+
+def ffblock_case():
+    """SysmatAssemblerFFBlock against matrix_blocked_ff (test/test_forms.jl,
+    module mbilform_diffusion_assembly_1): the block mesh, the nodes whose DOF
+    is fixed, and the tolerance."""
+    rel = "test/test_forms.jl"
+    txt, line = module_text(read(rel), "mbilform_diffusion_assembly_1", rel)
+    W, L, t = num(txt, "W"), num(txt, "L"), num(txt, "t")
+    sizes = dict(zip(["nl", "nt", "nw"], tuple_vals(txt, "nl, nt, nw")))
+    args = block_args(txt, "H8block")
+    env = {"W": W, "L": L, "t": t, **sizes}
+    fixed = re.search(r"nl = collect\((\d+):(\d+)\)", txt)
+    return {"source": f"{rel}:{line}",
+            "block": [env[a] for a in args[:3]] + [int(env[a]) for a in args[3:6]],
+            "gauss_order": int(re.search(r"GaussRule\(3,\s*(\d+)\)", txt).group(1)),
+            "fixed_nodes": list(range(int(fixed.group(1)), int(fixed.group(2)) + 1)),
+            "tol": 1.0e-5}
+
+
 def masslike_case():
     """bilform_masslike known answer (test/test_forms.jl, module
     mbilform_masslike_1): the L2 mesh's node coordinates, the Gauss order and
@@ -261,7 +307,8 @@ def main():
     if not os.path.isdir(REF):
         sys.exit(f"reference sources not found at {REF}")
     data = {"assembler": assembler_kats(), "patch": patch_tests(), **coloring_and_pattern(),
-            "conjugategradient": cg_case(), "masslike": masslike_case()}
+            "conjugategradient": cg_case(), "masslike": masslike_case(),
+            "div_grad": div_grad_cases(), "ffblock": ffblock_case()}
     with open(OUT, "w") as f:
         json.dump(data, f, indent=1)
     print("wrote", OUT)

@@ -798,3 +798,63 @@ def test_mixed_tensor_core_blocks(ft, et, monkeypatch):
         assert err_kx <= MIXED_TOL and err_max <= MIXED_TOL, (flag, err_kx, err_max)
         assert abs(K - K.T).max() == 0.0
     assert abs(out["1"] - out["0"]).max() > 0.0
+
+
+# ------------------------------------------------- reference identities on the GPU
+@pytest.mark.parametrize("idx", range(3))
+def test_div_grad_reference_identities(ft, kats, idx):
+    """test/test_forms.jl mbilform_div_grad_1..3 through the GPU entry point:
+    no energy for a constant velocity, 2 mu V |sym grad u|^2 for a linear
+    one, the elasticity energy with C = diag(2mu x3, mu x3) for a polynomial
+    one; the reference's default (unsymmetric) assembler."""
+    rec = kats["div_grad"][idx]
+    L, W, t, nl, nw, nt = rec["block"]
+    fens, fes = ft.H8block(L, W, t, nl, nw, nt)
+    femm = ft.FEMMBase(ft.IntegDomain(fes, ft.GaussRule(3, rec["gauss_order"])))
+    geom = ft.NodalField(fens.xyz)
+    u = _field(ft, fens.count(), 3)
+    mu, V, tol = rec["mu"], rec["volume"], rec["tol"]
+    G = ft.bilform_div_grad(femm, geom, u, ft.DataCache(mu))
+    x, y, z = fens.xyz[:, 0], fens.xyz[:, 1], fens.xyz[:, 2]
+    if rec["kind"] == "constant_field":
+        v = np.tile(rec["uxyz"], fens.count())
+        assert abs(v @ G @ v) / V <= tol
+        return
+    a, b, c, d = rec["abcd"]
+    if rec["kind"] == "linear_field":
+        U = np.stack([a + b * x + c * y + d * z, b + c * x + d * y + a * z,
+                      c + d * x + a * y + b * z], axis=1)
+        gradu = np.array([[b, c, d], [c, d, a], [d, a, b]])
+        exact = 2 * mu * V * (((gradu + gradu.T) / 2) ** 2).sum()
+        v = U.ravel()
+        assert abs(v @ G @ v - exact) / exact <= tol
+    else:
+        U = np.stack([a + b * x ** 2 + c * y ** 3 + d * z, b + c * x + d * y ** 2 + a * z ** 4,
+                      c + d * x ** 3 + a * y + b * z ** 2], axis=1)
+        C = np.diag([2 * mu] * 3 + [mu] * 3)
+        G2 = ft.bilform_lin_elastic(femm, geom, u, ft.DeforModelRed3D, ft.DataCache(C))
+        v = U.ravel()
+        e1, e2 = v @ G @ v, v @ G2 @ v
+        assert abs(e1 - e2) / e1 <= tol
+
+
+def test_ffblock_reference_case(ft, kats):
+    """test/test_forms.jl mbilform_diffusion_assembly_1: the free-free block by
+    SysmatAssemblerFFBlock equals matrix_blocked_ff of the full matrix (here
+    exactly, and the reference's energy check)."""
+    k = kats["ffblock"]
+    L, W, t, nl, nw, nt = k["block"]
+    fens, fes = ft.H8block(L, W, t, nl, nw, nt)
+    geom = ft.NodalField(fens.xyz)
+    psi = ft.NodalField(np.ones((fens.count(), 1)))
+    ft.setebc(psi, k["fixed_nodes"], True, [1] * len(k["fixed_nodes"]), 0.0)
+    ft.numberdofs(psi)
+    femm = ft.FEMMBase(ft.IntegDomain(fes, ft.GaussRule(3, k["gauss_order"])))
+    v_f = ft.gathersysvec(psi)
+    cf = ft.DataCache(np.eye(3))
+    K = ft.bilform_diffusion(femm, geom, psi, cf)
+    K_ff = ft.matrix_blocked_ff(K, psi.nfreedofs())
+    result = abs(v_f @ K_ff @ v_f)
+    B = ft.bilform_diffusion(femm, ft.SysmatAssemblerFFBlockGPU(psi.nfreedofs()), geom, psi, cf)
+    assert B.shape == K_ff.shape
+    assert abs(v_f @ B @ v_f - result) <= k["tol"] * max(result, 1e-300)

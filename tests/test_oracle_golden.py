@@ -279,3 +279,45 @@ def test_kat_masslike(O, kats):
     # SysmatAssemblerSparse keeps the explicit structure: one entry per
     # (element row, element DOF)
     assert G.nnz == conn.size
+
+
+def _div_grad_field(rec, xyz):
+    """The velocity fields of the reference's div_grad tests."""
+    x, y, z = xyz[:, 0], xyz[:, 1], xyz[:, 2]
+    if rec["kind"] == "constant_field":
+        return np.tile(rec["uxyz"], (xyz.shape[0], 1))
+    a, b, c, d = rec["abcd"]
+    if rec["kind"] == "linear_field":
+        return np.stack([a + b * x + c * y + d * z, b + c * x + d * y + a * z,
+                         c + d * x + a * y + b * z], axis=1)
+    return np.stack([a + b * x ** 2 + c * y ** 3 + d * z, b + c * x + d * y ** 2 + a * z ** 4,
+                     c + d * x ** 3 + a * y + b * z ** 2], axis=1)
+
+
+@pytest.mark.parametrize("idx", range(3))
+def test_kat_div_grad(O, kats, idx):
+    """bilform_div_grad identities of test/test_forms.jl (mbilform_div_grad_1
+    to _3): no energy for a constant velocity, 2 mu V |sym grad u|^2 for a
+    linear one, and the elasticity energy with C = diag(2mu x3, mu x3) for a
+    polynomial one."""
+    rec = kats["div_grad"][idx]
+    et, (xyz, conn) = O.H8, O.block(O.H8, *rec["block"])
+    pc, w = O.gauss_rule(3, rec["gauss_order"])
+    n, mu, V, tol = xyz.shape[0], rec["mu"], rec["volume"], rec["tol"]
+    dofs = np.arange(1, 3 * n + 1).reshape(n, 3)
+    G = O.bilform(O.DIV_GRAD, et, conn, xyz, dofs, 3 * n, pc, w, np.array([mu]),
+                  symmetric=False)
+    v = _div_grad_field(rec, xyz).ravel()
+    if rec["kind"] == "constant_field":
+        assert abs(v @ G @ v) / V <= tol
+    elif rec["kind"] == "linear_field":
+        a, b, c, d = rec["abcd"]
+        gradu = np.array([[b, c, d], [c, d, a], [d, a, b]])
+        sym = (gradu + gradu.T) / 2
+        exact = 2 * mu * V * (sym ** 2).sum()
+        assert abs(v @ G @ v - exact) / exact <= tol
+    else:
+        C = np.diag([2 * mu] * 3 + [mu] * 3)
+        G2 = O.bilform(O.LIN_ELASTIC, et, conn, xyz, dofs, 3 * n, pc, w, C)
+        e1, e2 = v @ G @ v, v @ G2 @ v
+        assert abs(e1 - e2) / e1 <= tol
