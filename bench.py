@@ -257,6 +257,33 @@ def pinned(torch, shape, dtype):
     return t.numpy().reshape(shape)
 
 
+def mixed_errors(K64, K32, seed=3):
+    """Error of a mixed-precision matrix against the FP64 one (same CSR
+    pattern): max |dK| / max |K|; max |dK_ij| / max_k |K_ik| (row scale); max
+    over nonzeros of |dK_ij| / |K_ij| raw (entries formed by cancellation,
+    near zero in FP64, make it large) and with a floor of 1e-12 max_k |K_ik|
+    in the row; |dK x| / |K x|."""
+    v64, v32 = K64.values(), K32.values()
+    d = np.abs(v32 - v64)
+    a = np.abs(v64)
+    rowptr, _ = K64.dm.pattern()
+    rowptr = rowptr - 1
+    counts = np.diff(rowptr)
+    rowmax = np.zeros(len(counts))
+    nz = counts > 0
+    rowmax[nz] = np.maximum.reduceat(a, rowptr[:-1][nz])
+    floor = np.repeat(1e-12 * rowmax, counts)
+    raw = d[a > 0] / a[a > 0]
+    x = np.random.default_rng(seed).uniform(-1, 1, K64.shape[0])
+    y64, y32 = K64.spmv(x), K32.spmv(x)
+    rowscale = np.repeat(np.where(rowmax > 0, rowmax, 1.0), counts)
+    return {"max_abs_over_max": float(d.max() / a.max()),
+            "max_abs_over_row_max": float((d / rowscale).max()),
+            "max_rel_nonzero_raw": float(raw.max()) if raw.size else 0.0,
+            "max_rel_nonzero_floor_1e-12_rowmax": float((d / np.maximum(a, floor)).max()),
+            "rel_Kx": float(np.linalg.norm(y32 - y64) / np.linalg.norm(y64))}
+
+
 def time_steps(torch, stream, fn, steps, warmup, flush=None, dist=None):
     """Device time of `steps` calls of fn on the library stream (CUDA events),
     barrier + synchronize on both sides; max over ranks."""
@@ -422,11 +449,33 @@ def run_ours(args):
                     for i in range(min(2, args.steps + args.warmup)))
     lib.nat.check(lib.L.fegpu_matrix_destroy(k2.value))
     lib.stats(reset=True)
+
+    workloads = {}
+    if not args.headline_only and args.only is None:
+        # the same T10 assembly in mixed precision (FP32 element blocks, row
+        # gather with float-float sums rounded once to FP64), and its error
+        K32 = ft.bilform_lin_elastic(femm, ft.SysmatAssemblerGPU(precision="mixed",
+                                                                 result="device", device=local),
+                                     geom, u, ft.DeforModelRed3D, ft.DataCache(D))
+
+        def mstep():
+            lib.nat.check(lib.L.fegpu_bilform_lin_elastic(K32.h, C.byref(coef), lib.nat.MIXED))
+
+        lib.stats(reset=True)
+        ms32 = time_steps(torch, stream, mstep, args.steps, args.warmup, dist=dist)
+        kms32, _ = lib.stats(reset=True)
+        workloads["t10_60_elasticity_mixed"] = {
+            "ms_per_step": ms32 / args.steps,
+            "elements_per_s": job_throughput(E, world, ms32 / args.steps * 1e-3),
+            "kernel_ms": kms32 / (args.steps + args.warmup),
+            "hbm_frac": B / (ms32 / args.steps * 1e-3) / 1e9 / peak,
+            "speedup_over_fp64": ms_step / (ms32 / args.steps),
+            "mixed_vs_fp64": mixed_errors(K, K32)}
+        del K32
     del K, asm
     femm = None
     torch.cuda.empty_cache()
 
-    workloads = {}
     if not args.headline_only and args.only is None:
         workloads["h20_40_elasticity"] = bench_h20(ft, torch, lib, stream, args, local, dist)
         workloads["h8_20_diffusion"] = bench_h8(ft, torch, lib, stream, args, local, dist)
@@ -538,14 +587,7 @@ def bench_h20(ft, torch, lib, stream, args, local, dist):
     v32 = mats["mixed"].values()
     res["mixed_persistent"]["identical_to_mixed"] = bool(np.array_equal(Mb.values(), v32))
     del b, Mb
-    v64 = mats["fp64"].values()
-    x = np.random.default_rng(3).uniform(-1, 1, mats["fp64"].shape[0])
-    y64 = mats["fp64"].spmv(x)
-    y32 = mats["mixed"].spmv(x)
-    res["mixed_vs_fp64"] = {
-        "max_abs_over_max": float(np.abs(v32 - v64).max() / np.abs(v64).max()),
-        "rel_Kx": float(np.linalg.norm(y32 - y64) / np.linalg.norm(y64)),
-    }
+    res["mixed_vs_fp64"] = mixed_errors(mats["fp64"], mats["mixed"])
     res["speedup_mixed_over_fp64"] = res["mixed"]["elements_per_s"] / res["fp64"]["elements_per_s"]
     return res
 
@@ -878,9 +920,22 @@ def bench_h8(ft, torch, lib, stream, args, local, dist):
     ms = time_steps(torch, stream, step, args.steps, args.warmup, flush=flush, dist=dist)
     lib.stats(reset=True)
     ms_step = ms / args.steps
-    return {"elements": fes.count(), "nnz": K.dm.nnz, "ms_per_step": ms_step,
-            "elements_per_s": fes.count() / (ms_step * 1e-3),
-            "l2": "flushed between steps (256 MB write)"}
+    out = {"elements": fes.count(), "nnz": K.dm.nnz, "ms_per_step": ms_step,
+           "elements_per_s": fes.count() / (ms_step * 1e-3),
+           "l2": "flushed between steps (256 MB write)"}
+    K32 = ft.bilform_diffusion(femm, ft.SysmatAssemblerGPU(precision="mixed", result="device",
+                                                           device=local),
+                               geom, u, ft.DataCache(1.0))
+
+    def mstep():
+        lib.nat.check(lib.L.fegpu_bilform_diffusion(K32.h, C.byref(coef), lib.nat.MIXED))
+
+    ms = time_steps(torch, stream, mstep, args.steps, args.warmup, flush=flush, dist=dist)
+    lib.stats(reset=True)
+    out["mixed"] = {"ms_per_step": ms / args.steps,
+                    "elements_per_s": fes.count() / (ms / args.steps * 1e-3)}
+    out["mixed_vs_fp64"] = mixed_errors(K, K32)
+    return out
 
 
 def main():
