@@ -46,7 +46,7 @@ template <> struct ElemT<FEGPU_T4> { static constexpr int NNE = 4, MDIM = 3; };
 template <> struct ElemT<FEGPU_T10> { static constexpr int NNE = 10, MDIM = 3; };
 
 struct SmemLayout {
-  size_t tab, X, G, WG, Jw, det, conn, pairs, ftab, fx, total;
+  size_t tab, X, G, WG, Jw, det, conn, pairs, total;
 };
 
 __host__ __device__ inline size_t align_up(size_t o, size_t a) { return (o + a - 1) / a * a; }
@@ -77,13 +77,6 @@ __host__ __device__ inline SmemLayout smem_layout(int nne, int mdim, int npts, i
   o += sizeof(int32_t) * te * nne;
   L.pairs = o;
   o += 2 * (nne * (nne + 1) / 2);
-  o = align_up(o, 16);
-  // FP32 copies for the mixed path: tables and element-relative coordinates
-  L.ftab = o;
-  if (tsize == 4) o += sizeof(float) * (npts * nne + npts * nne * mdim + npts);
-  o = align_up(o, 16);
-  L.fx = o;
-  if (tsize == 4) o += sizeof(float) * te * nne * 3;
   L.total = align_up(o, 16);
   return L;
 }
@@ -276,7 +269,6 @@ __global__ void __launch_bounds__(kFormThreads) k_form(const KArgs a) {
   constexpr int NNE = ElemT<ET>::NNE, MDIM = ElemT<ET>::MDIM;
   constexpr bool GRAD = FORM <= F_ELAST_GEN;
   constexpr int NBLK = NNE * (NNE + 1) / 2;
-  constexpr bool MIXED = std::is_same<T, float>::value;
   constexpr bool EXACT = !(FORM == F_ELAST_ISO || FORM == F_ELAST_GEN);
   extern __shared__ __align__(16) unsigned char smem[];
   const int npts = a.npts, te = a.te;
@@ -291,13 +283,10 @@ __global__ void __launch_bounds__(kFormThreads) k_form(const KArgs a) {
   float *sDet = reinterpret_cast<float *>(smem + L.det);
   int32_t *sConn = reinterpret_cast<int32_t *>(smem + L.conn);
   uint8_t *sPair = smem + L.pairs;
-  float *fdN = reinterpret_cast<float *>(smem + L.ftab) + npts * NNE;  // FP32 dN (mixed)
-  float *fX = reinterpret_cast<float *>(smem + L.fx);                 // FP32 relative coords
   const int tid = threadIdx.x, nth = blockDim.x;
 
   for (int i = tid; i < npts * NNE * (MDIM + 1) + npts; i += nth) {
     sN[i] = a.tab[i];
-    if constexpr (MIXED) reinterpret_cast<float *>(smem + L.ftab)[i] = float(a.tab[i]);
   }
   for (int i = tid; i < NBLK; i += nth) {
     int r = i, pa = 0;
@@ -325,51 +314,15 @@ __global__ void __launch_bounds__(kFormThreads) k_form(const KArgs a) {
       sX[3 * i + 2] = p[2];
     }
     __syncthreads();
-    if constexpr (MIXED) {
-      for (int i = tid; i < ne * NNE * 3; i += nth) {
-        const int e = i / (NNE * 3), r = i - e * NNE * 3;
-        fX[i] = float(sX[i] - sX[e * NNE * 3 + r % 3]);
-      }
-      __syncthreads();
-    }
 
     // ---- geometry per (element, quadrature point)
     for (int i = tid; i < ne * npts; i += nth) {
       const int e = i / npts, q = i - e * npts;
       T *g = sG + (static_cast<size_t>(e) * npts + q) * NNE * MDIM;
       T *wg = sWG + (static_cast<size_t>(e) * npts + q) * NNE * MDIM;
-      T Jac;
-      if constexpr (MIXED)
-        Jac = geometry_qp<NNE, MDIM, GRAD, float, T, EXACT>(fX + e * NNE * 3, fdN + q * NNE * MDIM,
-                                                          a.sdim, vol, a.otherdim, g,
-                                                          sDet + e * npts + q);
-      else
-        Jac = geometry_qp<NNE, MDIM, GRAD, double, T, EXACT>(sX + e * NNE * 3, sdN + q * NNE * MDIM,
-                                                           a.sdim, vol, a.otherdim, g,
-                                                           sDet + e * npts + q);
+      const T Jac = geometry_qp<NNE, MDIM, GRAD, double, T, EXACT>(
+          sX + e * NNE * 3, sdN + q * NNE * MDIM, a.sdim, vol, a.otherdim, g, sDet + e * npts + q);
       qp_weights<NNE, MDIM, FORM, T>(a, eb + e, q, npts, Jac, sw[q], g, wg, sJw + e * npts + q);
-    }
-    if constexpr (MIXED) {
-      // distorted elements (small det_min / det_max over the points): redo the
-      // Jacobian, its determinant and inverse in FP64
-      __syncthreads();
-      for (int i = tid; i < ne * npts; i += nth) {
-        const int e = i / npts, q = i - e * npts;
-        float dmin = 3.0e38f, dmax = 0.f;
-        for (int r = 0; r < npts; ++r) {
-          const float d = fabsf(sDet[e * npts + r]);
-          dmin = fminf(dmin, d);
-          dmax = fmaxf(dmax, d);
-        }
-        if (!(dmin > static_cast<float>(a.distort_tol) * dmax)) {
-          T *g = sG + (static_cast<size_t>(e) * npts + q) * NNE * MDIM;
-          T *wg = sWG + (static_cast<size_t>(e) * npts + q) * NNE * MDIM;
-          const T Jac = T(geometry_qp<NNE, MDIM, GRAD, double, T, EXACT>(
-              sX + e * NNE * 3, sdN + q * NNE * MDIM, a.sdim, vol, a.otherdim, g, nullptr));
-          qp_weights<NNE, MDIM, FORM, T>(a, eb + e, q, npts, Jac, sw[q], g, wg,
-                                         sJw + e * npts + q);
-        }
-      }
     }
     __syncthreads();
 
@@ -517,18 +470,6 @@ __global__ void __launch_bounds__(kFormThreads) k_form(const KArgs a) {
               Vt[ii][ii] = madd(f, sc, Vt[ii][ii]);
             }
           }
-        }
-      }
-
-      if constexpr (GRAD) {
-        if (a.ke) {
-          // ---- block output for the row gather: the (pa <= pb) block, row-major
-          float *kb = a.ke + (static_cast<int64_t>(eb + e - a.e0) * NBLK + blk) * (NDN * NDN);
-#pragma unroll
-          for (int ii = 0; ii < NDN; ++ii)
-#pragma unroll
-            for (int jj = 0; jj < NDN; ++jj) kb[ii * NDN + jj] = float(V[ii][jj]);
-          continue;
         }
       }
 
