@@ -13,9 +13,10 @@ from .batch import AssemblyBatch
 from .serve import AssemblyServer
 from .assembly import (DeviceMatrix, SysmatAssemblerGPU, SysmatAssemblerSparseDiagGPU,
                        SysmatAssemblerFFBlockGPU, SysmatAssemblerSparseHRZLumpingSymmGPU,
-                       SysvecAssemblerGPU, assemble,
-                       conjugategradient, makematrix, matrix_blocked_dd, matrix_blocked_df,
-                       matrix_blocked_fd, matrix_blocked_ff, startassembly)
+                       SysvecAssemblerFBlockGPU, SysvecAssemblerGPU, assemble,
+                       conjugategradient, makematrix, makevector, matrix_blocked_dd,
+                       matrix_blocked_df, matrix_blocked_fd, matrix_blocked_ff, startassembly,
+                       vector_blocked_d, vector_blocked_f)
 from .femm import (DataCache, DeforModelRed3D, ElementwiseData, FEMMBase, ForceIntensity,
                    IntegDomain, IsotropicElementwise, bilform_convection, bilform_diffusion, bilform_div_grad,
                    bilform_dot, bilform_masslike,

@@ -21,7 +21,8 @@ from . import _native as nat
 
 
 def _is_assembler(x) -> bool:
-    return isinstance(x, (SysmatAssemblerGPU, SysmatAssemblerFFBlockGPU, SysvecAssemblerGPU))
+    return isinstance(x, (SysmatAssemblerGPU, SysmatAssemblerFFBlockGPU, SysvecAssemblerGPU,
+                          SysvecAssemblerFBlockGPU))
 
 
 class DeviceMatrix:
@@ -262,15 +263,109 @@ def SysmatAssemblerSparseHRZLumpingSymmGPU(device: int = 0):
 
 
 class SysvecAssemblerGPU:
-    """GPU system-vector assembler (SysvecAssembler semantics)."""
+    """GPU system-vector assembler (SysvecAssembler semantics,
+    src/AssemblyModule.jl:853-917).  linform_dot / distribloads run on the
+    device; the generic protocol (startassembly / assemble / makevector) takes
+    element vectors from the caller and sums them on the device, each entry in
+    assembly order, through the generic COO assembler with one column."""
 
     def __init__(self, device: int = 0):
         self.device = device
+        self._generic = None
+        self._fin = None
+        self._n = 0
+
+    def eltype(self):
+        return np.float64
 
     def _run(self, dm, coef, m):
         F = np.zeros(dm.ndof)
         nat.check(nat.load().fegpu_linform_dot(dm.h, C.byref(coef), m, nat.ptr(F)))
+        return self._post(F)
+
+    def _post(self, F):
         return F
+
+    def startassembly(self, row_nalldofs):
+        if self._fin is not None:
+            self._fin()
+        out = C.c_void_p()
+        nat.check(nat.load().fegpu_assembler_create(nat.context(self.device), nat.ASM_SPARSE,
+                                                    int(row_nalldofs), 1, C.byref(out)))
+        self._generic = out.value
+        self._n = int(row_nalldofs)
+        self._fin = weakref.finalize(self, nat.load().fegpu_assembler_destroy, self._generic)
+        return self
+
+    def assemble(self, vec, dofnums):
+        if self._generic is None:
+            raise RuntimeError("startassembly must be called first")
+        v = np.ascontiguousarray(np.ravel(vec), dtype=np.float64)
+        r = np.ascontiguousarray(np.ravel(dofnums), dtype=np.int64)
+        if len(v) != len(r):
+            raise ValueError("Size mismatch")
+        one = np.ones(1, dtype=np.int64)
+        nat.check(nat.load().fegpu_assembler_assemble(self._generic, nat.ptr(v), len(r), 1,
+                                                      nat.ptr(r), nat.ptr(one)))
+        return self
+
+    def makevector(self):
+        nnz = C.c_int64()
+        nat.check(nat.load().fegpu_assembler_make(self._generic, C.byref(nnz)))
+        colptr = np.empty(2, dtype=np.int64)
+        rowval = np.empty(nnz.value, dtype=np.int64)
+        nzval = np.empty(nnz.value)
+        nat.check(nat.load().fegpu_assembler_copy_csc(self._generic, nat.ptr(colptr),
+                                                      nat.ptr(rowval), nat.ptr(nzval)))
+        F = np.zeros(self._n)
+        F[rowval - 1] = nzval
+        return self._post(F)
+
+
+class SysvecAssemblerFBlockGPU:
+    """SysvecAssemblerFBlock (src/AssemblyModule.jl:1238-1284): the vector
+    assembly of the wrapped GPU assembler, cut to the free DOFs
+    (vector_blocked_f)."""
+
+    def __init__(self, row_nfreedofs, a=None, device: int = 0):
+        self._a = a if a is not None else SysvecAssemblerGPU(device=device)
+        self._row_nfreedofs = int(row_nfreedofs)
+
+    def eltype(self):
+        return self._a.eltype()
+
+    def _post(self, F):
+        return vector_blocked_f(F, self._row_nfreedofs)
+
+    def _run(self, dm, coef, m):
+        return self._post(self._a._run(dm, coef, m))
+
+    def startassembly(self, row_nalldofs):
+        self._a.startassembly(row_nalldofs)
+        return self
+
+    def assemble(self, vec, dofnums):
+        self._a.assemble(vec, dofnums)
+        return self
+
+    def makevector(self):
+        return self._post(self._a.makevector())
+
+
+def vector_blocked_f(V, nfreedofs):
+    """vector_blocked_f (src/MatrixUtilityModule.jl:807-830): the free part."""
+    V = np.asarray(V)
+    if nfreedofs > V.shape[0]:
+        raise ValueError("The f block has too many rows")
+    return V[:nfreedofs].copy()
+
+
+def vector_blocked_d(V, nfreedofs):
+    """vector_blocked_d (src/MatrixUtilityModule.jl:832-855): the data part."""
+    V = np.asarray(V)
+    if nfreedofs > V.shape[0]:
+        raise ValueError("The f block has too many rows")
+    return V[nfreedofs:].copy()
 
 
 def _blocked(A, which, row_nfreedofs, col_nfreedofs):
@@ -331,3 +426,7 @@ def assemble(a, *args):
 
 def makematrix(a):
     return a.makematrix()
+
+
+def makevector(a):
+    return a.makevector()

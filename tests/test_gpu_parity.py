@@ -858,3 +858,47 @@ def test_ffblock_reference_case(ft, kats):
     B = ft.bilform_diffusion(femm, ft.SysmatAssemblerFFBlockGPU(psi.nfreedofs()), geom, psi, cf)
     assert B.shape == K_ff.shape
     assert abs(v_f @ B @ v_f - result) <= k["tol"] * max(result, 1e-300)
+
+
+def test_generic_vector_assembly(ft):
+    """SysvecAssembler's generic protocol (src/AssemblyModule.jl:885-917) on
+    the device: element vectors summed into the global vector in assembly
+    order (the same numbers as a host accumulation), bounds errors with the
+    reference's messages, and the free block (SysvecAssemblerFBlock)."""
+    rng = np.random.default_rng(12)
+    n = 57
+    a = ft.SysvecAssemblerGPU()
+    a.startassembly(n)
+    ref = np.zeros(n)
+    for _ in range(200):
+        k = int(rng.integers(1, 9))
+        v = rng.uniform(-1, 1, k)
+        d = rng.integers(1, n + 1, k)
+        a.assemble(v, d)
+        for vi, di in zip(v, d):
+            ref[di - 1] += vi
+    F = a.makevector()
+    assert np.array_equal(F, ref)
+    b = ft.SysvecAssemblerFBlockGPU(40)
+    b.startassembly(n)
+    b.assemble(np.array([1.0, 2.0]), np.array([3, 50]))
+    Fb = b.makevector()
+    assert Fb.shape == (40,) and Fb[2] == 1.0 and Fb.sum() == 1.0
+    a.startassembly(n)
+    with pytest.raises(ft.FegpuError, match="Row degree of freedom > size"):
+        a.assemble(np.array([1.0]), np.array([n + 1]))
+
+
+def test_linform_free_block(ft):
+    """linform_dot through SysvecAssemblerFBlock: the free part of the full
+    load vector."""
+    fens, fes = ft.H8block(1.0, 0.8, 0.6, 3, 3, 2)
+    femm = ft.FEMMBase(ft.IntegDomain(fes, ft.GaussRule(3, 2)))
+    geom = ft.NodalField(fens.xyz)
+    u = ft.NodalField(np.zeros((fens.count(), 3)))
+    ft.setebc(u, np.flatnonzero(np.abs(fens.xyz[:, 0]) < 1e-12) + 1, True, [1], 0.0)
+    ft.numberdofs(u)
+    f = ft.DataCache(np.array([1.0, -2.0, 0.5]))
+    F = ft.linform_dot(femm, geom, u, f, 3)
+    Ff = ft.linform_dot(femm, ft.SysvecAssemblerFBlockGPU(u.nfreedofs()), geom, u, f, 3)
+    assert np.array_equal(Ff, F[:u.nfreedofs()])

@@ -107,3 +107,14 @@ def test_element_coloring_restatement(ft, O):
     fens, fes = ft.T4block(1.0, 1.0, 1.0, 4, 3, 5)
     col, nc = O.element_coloring(fes.conn, fens.count())
     assert nc >= 1 and col.min() == 1
+
+
+def test_vector_blocked(ft):
+    """vector_blocked_f / _d (src/MatrixUtilityModule.jl:807-855): the free
+    and data parts; too many free DOFs is an error."""
+    v = np.arange(7.0)
+    assert np.array_equal(ft.vector_blocked_f(v, 3), v[:3])
+    assert np.array_equal(ft.vector_blocked_d(v, 3), v[3:])
+    assert ft.vector_blocked_f(v, 0).size == 0 and ft.vector_blocked_d(v, 7).size == 0
+    with pytest.raises(ValueError, match="too many rows"):
+        ft.vector_blocked_f(v, 8)
