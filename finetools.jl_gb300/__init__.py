@@ -17,7 +17,7 @@ from .assembly import (DeviceMatrix, SysmatAssemblerGPU, SysmatAssemblerSparseDi
                        conjugategradient, makematrix, makevector, matrix_blocked_dd,
                        matrix_blocked_df, matrix_blocked_fd, matrix_blocked_ff, startassembly,
                        vector_blocked_d, vector_blocked_f)
-from .femm import (DataCache, DeforModelRed3D, ElementwiseData, FEMMBase, ForceIntensity,
+from .femm import (CSys, DataCache, DeforModelRed3D, ElementwiseData, FEMMBase, ForceIntensity,
                    IntegDomain, IsotropicElementwise, bilform_convection, bilform_diffusion, bilform_div_grad,
                    bilform_dot, bilform_masslike,
                    bilform_lin_elastic, connectionmatrix, distribloads, innerproduct,

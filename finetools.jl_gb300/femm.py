@@ -120,13 +120,91 @@ class IntegDomain:
         return r.npts, Ns, dN, r.weights, pc
 
 
-class FEMMBase:
-    """Finite-element machine with the identity material frame
-    (src/FEMMBaseModule.jl:72-93).  Holds the device-resident element set
-    (connectivity, colouring, integration tables) once built."""
+class CSys:
+    """Material coordinate system (src/CSysModule.jl:17-110): CSys(dim) is the
+    identity; CSys(R) a constant rotation matrix R (columns: the material
+    axes in global coordinates), as csmat returns it.  A frame that varies
+    over the mesh (the reference's update function) is not taken by the
+    device forms: evaluate the rotated coefficient per point with a
+    DataCache fill function instead."""
 
-    def __init__(self, integdomain: IntegDomain, device: int = 0):
+    def __init__(self, spec):
+        if callable(spec):
+            raise NotImplementedError("a material frame that varies over the mesh: supply the "
+                                      "rotated coefficient per point (DataCache with a fill)")
+        if np.isscalar(spec):
+            self.csmat = np.eye(int(spec))
+        else:
+            self.csmat = np.array(spec, dtype=np.float64)
+            if self.csmat.ndim != 2 or self.csmat.shape[0] != self.csmat.shape[1]:
+                raise ValueError("CSys: a square rotation matrix")
+        self.isidentity = bool(np.array_equal(self.csmat, np.eye(self.csmat.shape[0])))
+
+
+def _strain_rotation(R):
+    """T with (local Voigt strain) = T (global Voigt strain), engineering
+    shears, order xx, yy, zz, xy, xz, yz: the strain that blmat! forms with
+    the gradients in the material frame and Rm (src/DeforModelRedModule.jl:
+    447-472) is R' eps R."""
+    T = np.zeros((6, 6))
+    for k in range(6):
+        e = np.zeros(6)
+        e[k] = 1.0
+        eps = np.array([[e[0], e[3] / 2, e[4] / 2], [e[3] / 2, e[1], e[5] / 2],
+                        [e[4] / 2, e[5] / 2, e[2]]])
+        loc = R.T @ eps @ R
+        T[:, k] = [loc[0, 0], loc[1, 1], loc[2, 2], 2 * loc[0, 1], 2 * loc[0, 2], 2 * loc[1, 2]]
+    return T
+
+
+def _is_isotropic_D(D):
+    """The 6 x 6 D of an isotropic material (invariant under rotation)."""
+    D = np.asarray(D).reshape(6, 6)
+    lam, mu = D[0, 1], D[3, 3]
+    iso = np.zeros((6, 6))
+    iso[:3, :3] = lam
+    iso[np.arange(3), np.arange(3)] = lam + 2 * mu
+    iso[np.arange(3, 6), np.arange(3, 6)] = mu
+    return bool(np.array_equal(D, iso))
+
+
+def _in_material_frame(femm, coef, keep, what):
+    """A coefficient given in the material frame of femm.mcsys, expressed in
+    global coordinates: K = sum B_l' D B_l with B_l = T B (elasticity: D ->
+    T' D T) and gradients g_l = g R (diffusion: kappa -> R kappa R').  The
+    identity frame, scalar conductivities and isotropic materials pass
+    unchanged."""
+    cs = femm.mcsys
+    if cs is None or cs.isidentity:
+        return coef
+    R = cs.csmat
+    v = keep[-1]
+    n = coef.ncomp
+    if what == "diffusion" and n == R.shape[0] ** 2:
+        rows = v.reshape(-1, n)
+        out = np.stack([(R @ r.reshape(R.shape) @ R.T).ravel() for r in rows])
+    elif what == "elasticity" and n == 36:
+        rows = v.reshape(-1, 36)
+        if all(_is_isotropic_D(r) for r in rows):
+            return coef
+        T = _strain_rotation(R)
+        out = np.stack([(T.T @ r.reshape(6, 6) @ T).ravel() for r in rows])
+    else:
+        return coef
+    out = np.ascontiguousarray(out.reshape(v.shape))
+    keep.append(out)
+    return nat.Coef(coef.kind, n, nat.ptr(out))
+
+
+class FEMMBase:
+    """Finite-element machine (src/FEMMBaseModule.jl:72-93): the integration
+    domain and the material frame (identity by default, or a constant
+    CSys).  Holds the device-resident element set (connectivity, colouring,
+    integration tables) once built."""
+
+    def __init__(self, integdomain: IntegDomain, mcsys: CSys = None, device: int = 0):
         self.integdomain = integdomain
+        self.mcsys = mcsys
         self.device = device
         self._h = None
         self._dofmaps = {}
@@ -274,7 +352,7 @@ def bilform_diffusion(femm: FEMMBase, *args):
     assembler = assembler or SysmatAssemblerGPU()
     dm = _prepare(femm, geom, u)
     keep = []
-    coef = _coef(femm, geom, cf, keep)
+    coef = _in_material_frame(femm, _coef(femm, geom, cf, keep), keep, "diffusion")
     return assembler._run(dm, lambda h: nat.load().fegpu_bilform_diffusion(
         h, C.byref(coef), assembler.precision_code))
 
@@ -287,7 +365,7 @@ def bilform_lin_elastic(femm: FEMMBase, *args):
     assembler = assembler or SysmatAssemblerGPU()
     dm = _prepare(femm, geom, u)
     keep = []
-    coef = _coef(femm, geom, cf, keep)
+    coef = _in_material_frame(femm, _coef(femm, geom, cf, keep), keep, "elasticity")
     return assembler._run(dm, lambda h: nat.load().fegpu_bilform_lin_elastic(
         h, C.byref(coef), assembler.precision_code))
 

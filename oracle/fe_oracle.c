@@ -845,13 +845,15 @@ static void grad_n(int nne, int mdim, const double *dN, const double *R, double 
 
 /* blmat!(DeforModelRed3D) with the identity material frame
  * (src/DeforModelRedModule.jl:447-472); B is 6 x 3nne row-major. */
-static void blmat3d(int nne, const double *g, double *B) {
+static void blmat3d(int nne, const double *g, const double *rm, double *B) {
   int n = 3 * nne;
   memset(B, 0, sizeof(double) * 6 * (size_t)n);
   for (int i = 0; i < nne; ++i)
     for (int j = 0; j < 3; ++j) {
       int kj = 3 * i + j;
-      double R1 = j == 0, R2 = j == 1, R3 = j == 2; /* Rm[j, :] of the identity */
+      /* Rm[j, :] (the identity when no material frame is given) */
+      double R1 = rm ? rm[3 * j] : (j == 0), R2 = rm ? rm[3 * j + 1] : (j == 1);
+      double R3 = rm ? rm[3 * j + 2] : (j == 2);
       const double *gi = g + 3 * i;
       B[0 * n + kj] = gi[0] * R1;
       B[1 * n + kj] = gi[1] * R2;
@@ -876,6 +878,19 @@ static double jac_mdim(const orc_problem *p, int mdim, const double *J, int m) {
   if (mdim == 2 && m == 3) return d * p->otherdim;
   if (mdim == 1 && m >= 2) return d * p->otherdim;
   return d;
+}
+
+/* Rm' J (mulCAtB!, src/MatrixUtilityModule.jl:478-521) for a 3-manifold in a
+ * constant material frame; J itself for the identity frame */
+static const double *rmtj(const orc_problem *p, int mdim, const double *J, double *out) {
+  if (!p->rm || mdim != 3) return J;
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b) {
+      double s = 0.0;
+      for (int k = 0; k < 3; ++k) s += p->rm[k * 3 + a] * J[k * 3 + b];
+      out[a * 3 + b] = s;
+    }
+  return out;
 }
 
 orc_matrix *orc_bilform(const orc_problem *p, int form, const orc_coef *c, int m,
@@ -910,7 +925,7 @@ orc_matrix *orc_bilform(const orc_problem *p, int form, const orc_coef *c, int m
   double *DB = (double *)malloc(sizeof(double) * 6 * n);
   double *kg = (double *)malloc(sizeof(double) * mdim * nne);
   int64_t *dofs = (int64_t *)malloc(sizeof(int64_t) * n);
-  double loc[3], J[9];
+  double loc[3], J[9], RmTJ[9];
   orc_assembler *a = orc_assembler_create(asm_kind, p->nalldofs, p->nalldofs);
   if (!a) return NULL;
   asm_reserve(a, p->nelem * (asm_kind == ORC_ASM_SPARSE_SYMM ? (int64_t)(n * n + n) / 2
@@ -928,8 +943,8 @@ orc_matrix *orc_bilform(const orc_problem *p, int form, const orc_coef *c, int m
       const double *cv = coef_at(c, e, q, npts);
       if (form == ORC_DIFFUSION) {
         double Jac = jac_mdim(p, mdim, J, 3);
-        grad_n(nne, mdim, dN, J, g); /* RmTJ = J for the identity frame */
         if (iso) {
+          grad_n(nne, mdim, dN, J, g); /* the iso form ignores the frame */
           /* add_mggt_ut_only! (src/MatrixUtilityModule.jl:84-98) */
           double mult = cv[0] * Jac * p->w[q];
           for (int nx = 0; nx < nne; ++nx)
@@ -938,6 +953,9 @@ orc_matrix *orc_bilform(const orc_problem *p, int form, const orc_coef *c, int m
               for (int mx = 0; mx <= nx; ++mx) Ke[mx * n + nx] += g[mx * mdim + px] * av;
             }
         } else {
+          /* RmTJ = Rm' J (src/FEMMBaseModule.jl:1495-1497), gradients in the
+           * material frame */
+          grad_n(nne, mdim, dN, rmtj(p, mdim, J, RmTJ), g);
           /* add_gkgt_ut_only! (src/MatrixUtilityModule.jl:120-153) */
           double Jw = Jac * p->w[q];
           for (int nx = 0; nx < nne; ++nx)
@@ -955,8 +973,9 @@ orc_matrix *orc_bilform(const orc_problem *p, int form, const orc_coef *c, int m
         }
       } else if (form == ORC_LIN_ELASTIC) {
         double Jac = jac_mdim(p, mdim, J, 3);
-        grad_n(nne, mdim, dN, J, g);
-        blmat3d(nne, g, B);
+        /* src/FEMMBaseModule.jl:1801-1804: RmTJ = Rm' J, blmat! with Rm */
+        grad_n(nne, mdim, dN, rmtj(p, mdim, J, RmTJ), g);
+        blmat3d(nne, g, p->rm, B);
         /* add_btdb_ut_only! (src/MatrixUtilityModule.jl:189-216) */
         double Jw = Jac * p->w[q];
         for (int nx = 0; nx < n; ++nx)

@@ -51,6 +51,8 @@ typedef struct {
   const double *pc;       /* npts x mdim parametric coordinates, row-major  */
   const double *w;        /* npts weights                                   */
   double otherdim;        /* constant "other dimension" (thickness)         */
+  const double *rm;       /* material frame: constant 3x3 rotation matrix,  */
+                          /* row-major (CSys csmat), or NULL = identity     */
 } orc_problem;
 
 typedef struct {

@@ -43,7 +43,7 @@ class _Problem(C.Structure):
         ("nnodes", C.c_int64), ("sdim", C.c_int), ("xyz", C.c_void_p),
         ("ndn", C.c_int), ("dofnums", C.c_void_p), ("nalldofs", C.c_int64),
         ("npts", C.c_int), ("pc", C.c_void_p), ("w", C.c_void_p),
-        ("otherdim", C.c_double),
+        ("otherdim", C.c_double), ("rm", C.c_void_p),
     ]
 
 
@@ -268,7 +268,7 @@ class Assembler:
             self.h = None
 
 
-def _problem(etype, conn, xyz, dofnums, nalldofs, pc, w, otherdim, keep):
+def _problem(etype, conn, xyz, dofnums, nalldofs, pc, w, otherdim, keep, rm=None):
     conn = np.ascontiguousarray(conn, dtype=np.int64)
     xyz = np.ascontiguousarray(xyz, dtype=np.float64)
     dofnums = np.ascontiguousarray(dofnums, dtype=np.int64)
@@ -277,9 +277,14 @@ def _problem(etype, conn, xyz, dofnums, nalldofs, pc, w, otherdim, keep):
     pc = np.ascontiguousarray(pc, dtype=np.float64)
     w = np.ascontiguousarray(w, dtype=np.float64)
     keep += [conn, xyz, dofnums, pc, w]
+    rmp = None
+    if rm is not None:
+        rm = np.ascontiguousarray(rm, dtype=np.float64).reshape(3, 3)
+        keep.append(rm)
+        rmp = _p(rm)
     return _Problem(etype, conn.shape[0], _p(conn), xyz.shape[0], xyz.shape[1], _p(xyz),
                     dofnums.shape[1], _p(dofnums), int(nalldofs), len(w), _p(pc), _p(w),
-                    float(otherdim))
+                    float(otherdim), rmp)
 
 
 def _coef(kind, data, keep):
@@ -296,14 +301,14 @@ def _coef(kind, data, keep):
 
 
 def bilform(form, etype, conn, xyz, dofnums, nalldofs, pc, w, coef, coef_kind=COEF_CONST,
-            otherdim=1.0, m=3, symmetric=True, phases=False, asm=None):
+            otherdim=1.0, m=3, symmetric=True, phases=False, asm=None, rm=None):
     """One bilinear form, assembled like the reference's 4/5-argument call.
 
     Returns the scipy CSC matrix (and, optionally, the number of exact zeros
     dropped by the symmetric completion and the phase timings).
     """
     keep = []
-    P = _problem(etype, conn, xyz, dofnums, nalldofs, pc, w, otherdim, keep)
+    P = _problem(etype, conn, xyz, dofnums, nalldofs, pc, w, otherdim, keep, rm)
     Cf = _coef(coef_kind, coef, keep)
     ph = np.zeros(3)
     kind = asm if asm is not None else (ASM_SPARSE_SYMM if symmetric else ASM_SPARSE)

@@ -902,3 +902,42 @@ def test_linform_free_block(ft):
     F = ft.linform_dot(femm, geom, u, f, 3)
     Ff = ft.linform_dot(femm, ft.SysvecAssemblerFBlockGPU(u.nfreedofs()), geom, u, f, 3)
     assert np.array_equal(Ff, F[:u.nfreedofs()])
+
+
+@pytest.mark.parametrize("form", ["diffusion", "elasticity"])
+def test_material_frame(ft, O, form):
+    """A constant material frame (CSys with a rotation matrix,
+    src/CSysModule.jl): the oracle follows the reference (gradients in the
+    frame, RmTJ = Rm' J, blmat! with Rm); the device forms take the
+    coefficient rotated to global coordinates."""
+    rng = np.random.default_rng(23)
+    fens, fes = ft.H8block(1.0, 0.7, 1.3, 3, 2, 2)
+    fens.xyz = ft.meshes.jitter_interior(fens.xyz, (3, 2, 2), 0.15, 5, box=(1.0, 0.7, 1.3))
+    Q, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+    R = Q * np.sign(np.linalg.det(Q))           # a proper rotation
+    femm = ft.FEMMBase(ft.IntegDomain(fes, ft.GaussRule(3, 2)), mcsys=ft.CSys(R))
+    geom = ft.NodalField(fens.xyz)
+    npts, Ns, dN, w, pc = femm.integdomain.integrationdata()
+    if form == "diffusion":
+        kap = np.diag([3.0, 1.0, 0.2])
+        kap[0, 1] = kap[1, 0] = 0.4
+        u = _field(ft, fens.count(), 1)
+        K = ft.bilform_diffusion(femm, geom, u, ft.DataCache(kap))
+        Kr = O.bilform(O.DIFFUSION, fes.code, fes.conn, geom.values, u.dofnums, u.nalldofs(),
+                       pc, w, kap, rm=R)
+    else:
+        D = np.zeros((6, 6))
+        D[:3, :3] = [[12.0, 3.0, 2.0], [3.0, 9.0, 2.5], [2.0, 2.5, 7.0]]
+        D[3, 3], D[4, 4], D[5, 5] = 3.0, 2.0, 2.6
+        u = _field(ft, fens.count(), 3)
+        K = ft.bilform_lin_elastic(femm, geom, u, ft.DeforModelRed3D, ft.DataCache(D))
+        Kr = O.bilform(O.LIN_ELASTIC, fes.code, fes.conn, geom.values, u.dofnums,
+                       u.nalldofs(), pc, w, D, rm=R)
+    compare(K, Kr, structure=False)
+    # the frame matters: the identity frame gives another matrix
+    femm0 = ft.FEMMBase(ft.IntegDomain(fes, ft.GaussRule(3, 2)))
+    if form == "diffusion":
+        K0 = ft.bilform_diffusion(femm0, geom, u, ft.DataCache(kap))
+    else:
+        K0 = ft.bilform_lin_elastic(femm0, geom, u, ft.DeforModelRed3D, ft.DataCache(D))
+    assert abs(K - K0).max() > 1e-3 * abs(K).max()
