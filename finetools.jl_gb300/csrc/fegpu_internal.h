@@ -67,11 +67,15 @@ inline int nodes_per_elem(int et) {
   return 0;
 }
 inline int manif_dim(int et) { return et == FEGPU_Q4 ? 2 : 3; }
+// quadrature points accepted per element type: the reference's Gauss rules of
+// orders 1-10 (tensor products) and tet rules of 1, 4 and 5 points; rules
+// whose per-element tables do not fit a kernel's shared memory are refused
+// when the form runs
 inline int max_qp(int et) {
   switch (et) {
-    case FEGPU_Q4: return 16;
-    case FEGPU_H8: return 27;
-    case FEGPU_H20: return 27;
+    case FEGPU_Q4: return 100;
+    case FEGPU_H8: return 1000;
+    case FEGPU_H20: return 1000;
     case FEGPU_T4: return 5;
     case FEGPU_T10: return 5;
   }

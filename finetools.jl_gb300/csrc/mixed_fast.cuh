@@ -448,9 +448,14 @@ inline size_t tile_smem_bytes(int etype, int form, int npts, int te) {
   return mixed_layout(nne, manif_dim(etype), npts, te).total;
 }
 
+// elements per tile; rules with many points (Gauss orders above 3) get fewer
+// elements so that a tile's tables stay within a CTA's shared memory
 inline int default_tile(int etype, int form, int npts) {
-  if (form == F_DIFF_ISO || form == F_ELAST_ISO || form == F_DOT) return default_fast_tile(etype);
-  return default_general_tile(etype, npts);
+  int te = (form == F_DIFF_ISO || form == F_ELAST_ISO || form == F_DOT)
+               ? default_fast_tile(etype)
+               : default_general_tile(etype, npts);
+  while (te > 1 && tile_smem_bytes(etype, form, npts, te) > 200 * 1024) --te;
+  return te;
 }
 
 template <int ET, int FORM, int NDN>

@@ -941,3 +941,60 @@ def test_material_frame(ft, O, form):
     else:
         K0 = ft.bilform_lin_elastic(femm0, geom, u, ft.DeforModelRed3D, ft.DataCache(D))
     assert abs(K - K0).max() > 1e-3 * abs(K).max()
+
+
+@pytest.mark.parametrize("et,form,order", [("H8", "elasticity", 4), ("H20", "diffusion", 4),
+                                           ("H8", "diffusion", 6), ("Q4", "dot", 6)])
+def test_high_order_gauss_rules(ft, O, et, form, order):
+    """Gauss rules beyond order 3 (the reference tabulates orders 1-10): the
+    FP64 forms against the oracle with the same tables, and the mixed path
+    (smaller tiles for the larger tables) within the mixed bound."""
+    rng = np.random.default_rng(31)
+    if et == "Q4":
+        fens, fes = ft.Q4block(2.0, 1.5, 5, 4)
+        xyz = np.hstack([fens.xyz, rng.uniform(-0.05, 0.05, (fens.count(), 1))])
+        femm = ft.FEMMBase(ft.IntegDomain(fes, ft.GaussRule(2, order), 0.01))
+    else:
+        gen = ft.H8block if et == "H8" else ft.H20block
+        fens, fes = gen(1.0, 0.7, 1.3, 3, 2, 2)
+        xyz = ft.meshes.jitter_interior(fens.xyz, (3, 2, 2), 0.15, 4, box=(1.0, 0.7, 1.3))
+        if et == "H20":
+            fens.xyz = xyz
+            xyz = ft.meshes.recompute_midpoints(fens, fes, 0).xyz
+        femm = ft.FEMMBase(ft.IntegDomain(fes, ft.GaussRule(3, order)))
+    geom = ft.NodalField(xyz)
+    npts, Ns, dN, w, pc = femm.integdomain.integrationdata()
+    assert npts == order ** (2 if et == "Q4" else 3)
+    od = femm.integdomain.otherdimension
+    if form == "elasticity":
+        u = _field(ft, fens.count(), 3)
+        D = ft.isotropic_D(1.0, 0.3)
+        K = ft.bilform_lin_elastic(femm, geom, u, ft.DeforModelRed3D, ft.DataCache(D))
+        Kr = O.bilform(O.LIN_ELASTIC, fes.code, fes.conn, geom.values, u.dofnums, u.nalldofs(),
+                       pc, w, D)
+        K32 = ft.bilform_lin_elastic(femm, ft.SysmatAssemblerGPU(precision="mixed"), geom, u,
+                                     ft.DeforModelRed3D, ft.DataCache(D))
+        x = rng.uniform(-1, 1, K.shape[0])
+        assert np.linalg.norm((K32 - K) @ x) <= MIXED_TOL * np.linalg.norm(K @ x)
+    elif form == "diffusion":
+        u = _field(ft, fens.count(), 1)
+        K = ft.bilform_diffusion(femm, geom, u, ft.DataCache(1.3))
+        Kr = O.bilform(O.DIFFUSION, fes.code, fes.conn, geom.values, u.dofnums, u.nalldofs(),
+                       pc, w, np.array([1.3]))
+    else:
+        u = _field(ft, fens.count(), 1)
+        K = ft.bilform_dot(femm, geom, u, ft.DataCache(np.eye(1) * 2.0))
+        Kr = O.bilform(O.DOT, fes.code, fes.conn, geom.values, u.dofnums, u.nalldofs(), pc, w,
+                       np.eye(1) * 2.0, otherdim=od, m=3)
+    compare(K, Kr)
+
+
+def test_rule_too_large_is_refused(ft):
+    """A rule whose per-element tables exceed a CTA's shared memory is refused
+    with an error, not run."""
+    fens, fes = ft.H20block(1.0, 1.0, 1.0, 2, 2, 2)
+    femm = ft.FEMMBase(ft.IntegDomain(fes, ft.GaussRule(3, 10)))
+    u = _field(ft, fens.count(), 3)
+    with pytest.raises(ft.FegpuError, match="too large"):
+        ft.bilform_lin_elastic(femm, ft.NodalField(fens.xyz), u, ft.DeforModelRed3D,
+                               ft.DataCache(ft.isotropic_D(1.0, 0.3)))
