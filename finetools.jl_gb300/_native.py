@@ -24,7 +24,7 @@ EXPORTS = [
     "fegpu_last_error", "fegpu_context_create", "fegpu_context_destroy",
     "fegpu_context_synchronize", "fegpu_context_stream", "fegpu_context_timing",
     "fegpu_context_kernel_stats", "fegpu_femm_create", "fegpu_femm_destroy",
-    "fegpu_femm_set_geometry", "fegpu_femm_colors", "fegpu_dofmap_create",
+    "fegpu_femm_set_geometry", "fegpu_femm_set_axisymmetric", "fegpu_femm_colors", "fegpu_dofmap_create",
     "fegpu_dofmap_destroy", "fegpu_dofmap_copy_pattern", "fegpu_matrix_create",
     "fegpu_matrix_destroy", "fegpu_bilform_diffusion", "fegpu_bilform_lin_elastic",
     "fegpu_bilform_dot", "fegpu_bilform_div_grad", "fegpu_bilform_convection", "fegpu_linform_dot", "fegpu_bilform_dot_lumped", "fegpu_matrix_nnz", "fegpu_matrix_copy_csc",
@@ -75,6 +75,7 @@ def load(path: str = LIBPATH):
         "fegpu_femm_create": ([vp, i32, i64, vp, i64, i32, vp, vp, vp, d, pp], i32),
         "fegpu_femm_destroy": ([vp], i32),
         "fegpu_femm_set_geometry": ([vp, i32, vp], i32),
+        "fegpu_femm_set_axisymmetric": ([vp, i32], i32),
         "fegpu_femm_colors": ([vp, vp, p64], i32),
         "fegpu_dofmap_create": ([vp, i32, vp, i64, pp, p64], i32),
         "fegpu_dofmap_destroy": ([vp], i32),

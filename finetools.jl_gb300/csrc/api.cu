@@ -224,6 +224,7 @@ KArgs base_args(fegpu_matrix *K, fegpu_dofmap *dm) {
   a.npts = fm->npts;
   a.sdim = fm->sdim;
   a.otherdim = fm->otherdim;
+  a.axisym = fm->axisym;
   a.measure_m = 3;
   // mixed path: elements whose det J ratio over the points falls below this
   // take FP64 Jacobians.  T10 takes them always: its FP32 Jacobian sums ten
@@ -578,6 +579,13 @@ int fegpu_femm_destroy(fegpu_femm *femm) {
     cudaSetDevice(femm->ctx->device);
     cudaStreamSynchronize(femm->ctx->stream);
     delete femm;
+  });
+}
+
+int fegpu_femm_set_axisymmetric(fegpu_femm *fm, int axisymmetric) {
+  return guarded([&] {
+    FEGPU_REQUIRE(fm, "null handle");
+    fm->axisym = axisymmetric ? 1 : 0;
   });
 }
 

@@ -19,7 +19,8 @@ template <int NNE, int MDIM>
 __global__ void k_convection(const int32_t *conn, const double *xyz, const double *vel,
                              const double *tab, int npts, const uint16_t *pos, const int32_t *dof,
                              const int64_t *rowptr, const int32_t *colperm, const int64_t *cpoff,
-                             double otherdim, double *val, int64_t e0, int64_t e1) {
+                             double otherdim, int axisym, double *val, int64_t e0,
+                             int64_t e1) {
   const double *N = tab;
   const double *dN = tab + npts * NNE;
   const double *w = dN + npts * NNE * MDIM;
@@ -75,7 +76,15 @@ __global__ void k_convection(const int32_t *conn, const double *xyz, const doubl
         inv[1][1] = J[0][0] * id;
       }
       // Jacobianvolume: a two-manifold is scaled by the other dimension
-      const double Jw = (MDIM == 2 ? det * otherdim : det) * w[q];
+      // Jacobianvolume: a two-manifold is scaled by the other dimension, or by
+      // 2 pi r on an axisymmetric domain
+      double od = otherdim;
+      if (MDIM == 2 && axisym) {
+        double r = 0.0;
+        for (int k = 0; k < NNE; ++k) r = fma(Nq[k], xyz[4 * static_cast<int64_t>(ce[k])], r);
+        od = 2.0 * 3.14159265358979323846 * r;
+      }
+      const double Jw = (MDIM == 2 ? det * od : det) * w[q];
       // (u . grad N_r) for every r
       double ug[NNE];
 #pragma unroll
@@ -127,7 +136,8 @@ void launch_convection(const fegpu_femm *fm, const fegpu_dofmap *dm, const doubl
         fm->conn.as<int32_t>(), fm->xyz.as<double>(), vel4, fm->tab.as<double>(), fm->npts,
         dm->pos.as<uint16_t>(), dm->dof.as<int32_t>(), dm->rowptr.as<int64_t>(),
         dm->contiguous ? nullptr : dm->colperm.as<int32_t>(),
-        dm->contiguous ? nullptr : dm->cpoff.as<int64_t>(), fm->otherdim, val, e0, e1);
+        dm->contiguous ? nullptr : dm->cpoff.as<int64_t>(), fm->otherdim, fm->axisym, val, e0,
+        e1);
     FEGPU_CUDA(cudaGetLastError());
   }
 }

@@ -124,7 +124,8 @@ __device__ __forceinline__ C madd(C a, C b, C c) {  // c + a*b
 template <int NNE, int MDIM, bool GRAD, typename C, typename T, bool EX = true, typename XT>
 __device__ __forceinline__ C geometry_qp(const XT *X, const XT *dN, int sdim,
                                          int measure_volume, double otherdim, T *g,
-                                         float *det_out) {
+                                         float *det_out, const XT *Nq = nullptr,
+                                         int axisym = 0) {
   // coordinates: absolute in FP64; in FP32 relative to the element's first
   // node (computed once per element: the gradients of the basis sum to zero,
   // so J is unchanged)
@@ -184,7 +185,18 @@ __device__ __forceinline__ C geometry_qp(const XT *X, const XT *dN, int sdim,
       inv[1][0] = mul<C, EX>(-J[1][0], id);
       inv[1][1] = mul<C, EX>(J[0][0], id);
     }
-    if (measure_volume) Jac = mul<C, EX>(Jac, C(otherdim));
+    if (measure_volume) {
+      if (axisym) {
+        // Jacobianvolume on an axisymmetric domain: Jac * 2 * pi * loc[1]
+        // (src/IntegDomainModule.jl:521-549), loc = N' X
+        C r = C(0);
+#pragma unroll
+        for (int k = 0; k < NNE; ++k) r = madd<C, EX>(C(Nq[k]), C(X[3 * k]), r);
+        Jac = mul<C, EX>(mul<C, EX>(mul<C, EX>(Jac, C(2)), C(3.14159265358979323846)), r);
+      } else {
+        Jac = mul<C, EX>(Jac, C(otherdim));
+      }
+    }
   }
   if (det_out) *det_out = float(Jac);
   if (GRAD) {
@@ -321,7 +333,8 @@ __global__ void __launch_bounds__(kFormThreads) k_form(const KArgs a) {
       T *g = sG + (static_cast<size_t>(e) * npts + q) * NNE * MDIM;
       T *wg = sWG + (static_cast<size_t>(e) * npts + q) * NNE * MDIM;
       const T Jac = geometry_qp<NNE, MDIM, GRAD, double, T, EXACT>(
-          sX + e * NNE * 3, sdN + q * NNE * MDIM, a.sdim, vol, a.otherdim, g, sDet + e * npts + q);
+          sX + e * NNE * 3, sdN + q * NNE * MDIM, a.sdim, vol, a.otherdim, g, sDet + e * npts + q,
+          sN + q * NNE, a.axisym);
       qp_weights<NNE, MDIM, FORM, T>(a, eb + e, q, npts, Jac, sw[q], g, wg, sJw + e * npts + q);
     }
     __syncthreads();

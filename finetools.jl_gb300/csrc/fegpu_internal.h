@@ -110,6 +110,7 @@ struct fegpu_femm {
   int etype = 0, nne = 0, mdim = 0, npts = 0, sdim = 0;
   int64_t nelem = 0, nnodes = 0;
   double otherdim = 1.0;
+  int axisym = 0;                      // axisymmetric domain (two-manifolds: 2 pi r)
   std::vector<int64_t> colors;         // element order, 1-based
   std::vector<int64_t> color_offsets;  // sorted-element ranges per colour
   fegpu::DevBuf conn_orig;             // int32 nelem x nne, 0-based, element order
@@ -199,6 +200,7 @@ struct KArgs {
   int npts, sdim, te;
   int measure_m;           // manifold dimension of the measure (dot, linform)
   double otherdim;
+  int axisym;              // axisymmetric domain: 2 pi r instead of otherdim
   double distort_tol;      // mixed path: det_min/det_max below -> FP64 geometry
   int64_t e0, e1;          // colour range of sorted elements
   int *status;             // device status word (0 = ok)

@@ -17,7 +17,7 @@ namespace {
 
 template <int NNE, int MDIM, int NDN>
 __global__ void k_lumped_dot(const int32_t *conn, const double *xyz, const double *tab, int npts,
-                             int sdim, double otherdim, int measure_m, int coef_kind,
+                             int sdim, double otherdim, int axisym, int measure_m, int coef_kind,
                              const double *cconst, const double *coef, const int32_t *dof,
                              int64_t e0, int64_t e1, int hrz, double *diag) {
   const double *N = tab;
@@ -35,7 +35,8 @@ __global__ void k_lumped_dot(const int32_t *conn, const double *xyz, const doubl
     for (int q = 0; q < npts; ++q) {
       double J[3][MDIM];
       jacobian_matrix<NNE, MDIM>(ce, xyz, dN + q * NNE * MDIM, J);
-      const double Jac = jacobian_mdim<MDIM>(J, sdim, otherdim, measure_m);
+      const double rad = (MDIM == 2 && axisym) ? point_r<NNE>(ce, xyz, N + q * NNE) : 0.0;
+      const double Jac = jacobian_mdim<MDIM>(J, sdim, otherdim, measure_m, axisym, rad);
       // coefficient c[p][q] at this point
       double c[NDN][NDN];
 #pragma unroll
@@ -95,7 +96,8 @@ void launch_lumped(const fegpu_femm *fm, const fegpu_dofmap *dm, const double *c
     const int grid = static_cast<int>(std::min<int64_t>((e1 - e0 + 127) / 128, 4096));
     k_lumped_dot<NNE, MDIM, NDN><<<grid, 128, 0, s>>>(
         fm->conn.as<int32_t>(), fm->xyz.as<double>(), fm->tab.as<double>(), fm->npts, fm->sdim,
-        fm->otherdim, m, coef_kind, cconst, coef, dm->dof.as<int32_t>(), e0, e1, hrz, diag);
+        fm->otherdim, fm->axisym, m, coef_kind, cconst, coef, dm->dof.as<int32_t>(), e0, e1, hrz,
+        diag);
     FEGPU_CUDA(cudaGetLastError());
   }
 }

@@ -21,9 +21,9 @@ namespace {
 
 template <int NNE, int MDIM, int NDN>
 __global__ void k_masslike(const int32_t *conn, const double *xyz, const double *tab, int npts,
-                           int sdim, double otherdim, int measure_m, int coef_kind, int ncomp,
-                           const double *coef, const int32_t *dof, int64_t nelem, uint64_t *key,
-                           int64_t *idx, double *V) {
+                           int sdim, double otherdim, int axisym, int measure_m, int coef_kind,
+                           int ncomp, const double *coef, const int32_t *dof, int64_t nelem,
+                           uint64_t *key, int64_t *idx, double *V) {
   const double *N = tab;
   const double *dN = tab + npts * NNE;
   const double *w = dN + npts * NNE * MDIM;
@@ -39,7 +39,8 @@ __global__ void k_masslike(const int32_t *conn, const double *xyz, const double 
     for (int q = 0; q < npts; ++q) {
       double J[3][MDIM];
       jacobian_matrix<NNE, MDIM>(ce, xyz, dN + q * NNE * MDIM, J);
-      const double Jac = jacobian_mdim<MDIM>(J, sdim, otherdim, measure_m);
+      const double rad = (MDIM == 2 && axisym) ? point_r<NNE>(ce, xyz, N + q * NNE) : 0.0;
+      const double Jac = jacobian_mdim<MDIM>(J, sdim, otherdim, measure_m, axisym, rad);
       // c[p][r] at (element e, point q): constant, per element or per point;
       // a scalar stands for that multiple of the identity
       const double *cv = coef_kind == FEGPU_COEF_CONST ? coef
@@ -86,8 +87,8 @@ void launch_masslike(const fegpu_femm *fm, const fegpu_dofmap *dm, int m, int ki
   const int grid = static_cast<int>(std::min<int64_t>((fm->nelem + 127) / 128, 4096));
   k_masslike<NNE, MDIM, NDN><<<grid, 128, 0, s>>>(
       fm->conn_orig.as<int32_t>(), fm->xyz.as<double>(), fm->tab.as<double>(), fm->npts,
-      fm->sdim, fm->otherdim, m, kind, ncomp, coef, dm->dof.as<int32_t>(), fm->nelem, key, idx,
-      V);
+      fm->sdim, fm->otherdim, fm->axisym, m, kind, ncomp, coef, dm->dof.as<int32_t>(),
+      fm->nelem, key, idx, V);
   FEGPU_CUDA(cudaGetLastError());
 }
 

@@ -250,7 +250,16 @@ __device__ __forceinline__ void mixed_tile(const KArgs &a, int64_t eb, int ne,
         det = float(dd);
       }
       float w = det * fw[q];
-      if (MDIM == 2 && (GRAD || a.measure_m == 3)) w *= odim;
+      if (MDIM == 2 && (GRAD || a.measure_m == 3)) {
+        if (a.axisym) {  // 2 pi r from the first node and the relative coordinates
+          float r = 0.f;
+          for (int k = 0; k < NNE; ++k) r = fmaf(fN[q * NNE + k], fX[3 * (e * NNE + k)], r);
+          r += float(a.xyz[4 * static_cast<int64_t>(sConn[e * NNE])]);
+          w *= 2.f * 3.14159265f * r;
+        } else {
+          w *= odim;
+        }
+      }
       if constexpr (FORM == F_DIFF_ISO || FORM == F_DOT) {
         float c = 1.f;
         if (a.coef_kind == FEGPU_COEF_CONST) c = float(a.cconst[0]);

@@ -98,6 +98,7 @@ __device__ __forceinline__ void fast_geometry(const KArgs &a, int64_t eb, int ne
   constexpr int NNE = ElemT<ET>::NNE, MDIM = ElemT<ET>::MDIM;
   constexpr bool GRAD = FORM != F_DOT;
   const int npts = a.npts;
+  const float *fN = a.tab32;
   const float *fdN = a.tab32 + npts * NNE;
   const float *fw = fdN + npts * NNE * MDIM;
   const int tid = threadIdx.x, nth = blockDim.x;
@@ -208,7 +209,16 @@ __device__ __forceinline__ void fast_geometry(const KArgs &a, int64_t eb, int ne
       }
     }
     float w = det * fw[q];
-    if (MDIM == 2 && (GRAD || a.measure_m == 3)) w *= odim;
+    if (MDIM == 2 && (GRAD || a.measure_m == 3)) {
+      if (a.axisym) {  // 2 pi r, r from the element's first node and the relative coordinates
+        float r = 0.f;
+        for (int k = 0; k < NNE; ++k) r = fmaf(fN[q * NNE + k], fX[e * NNE + k].x, r);
+        r += float(a.xyz[4 * static_cast<int64_t>(sConn[e * NNE])]);
+        w *= 2.f * 3.14159265f * r;
+      } else {
+        w *= odim;
+      }
+    }
     if constexpr (FORM == F_DIFF_ISO || FORM == F_DOT) {
       float c = 1.f;
       if (a.coef_kind == FEGPU_COEF_CONST) c = float(a.cconst[0]);

@@ -97,15 +97,17 @@ class ForceIntensity:
 
 
 class IntegDomain:
-    """Element set + integration rule + other dimension
-    (src/IntegDomainModule.jl:43-143).  Only constant other dimensions are
-    supported on the GPU."""
+    """Element set + integration rule + other dimension, or an axisymmetric
+    domain (src/IntegDomainModule.jl:43-143): a two-manifold measured as a
+    volume is scaled by the constant other dimension or by 2 pi r.  Only
+    constant other dimensions are supported on the GPU."""
 
     def __init__(self, fes, integration_rule, otherdimension=1.0, axisymmetric=False):
         if callable(otherdimension):
             raise NotImplementedError("the GPU path supports a constant other dimension")
-        if axisymmetric:
-            raise NotImplementedError("axisymmetric integration domains are not supported")
+        if isinstance(otherdimension, bool):  # IntegDomain(fes, rule, axisymmetric)
+            otherdimension, axisymmetric = 1.0, otherdimension
+        self.axisymmetric = bool(axisymmetric)
         self.fes = fes
         self.integration_rule = integration_rule
         self.otherdimension = float(otherdimension)
@@ -233,6 +235,8 @@ class FEMMBase:
             self._h = h.value
             self._nnodes = nnodes
             weakref.finalize(self, _destroy, "fegpu_femm_destroy", self._h, self._dofmaps)
+            if self.integdomain.axisymmetric:
+                nat.check(L.fegpu_femm_set_axisymmetric(self._h, 1))
         return self._h
 
     def _ensure_nodes(self, nnodes):

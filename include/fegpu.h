@@ -107,6 +107,11 @@ int fegpu_femm_destroy(fegpu_femm *femm);
 /* geometry NodalField values (nnodes x sdim, column-major), uploaded and kept
  * resident; call again to move the nodes (re-assembly on new coordinates). */
 int fegpu_femm_set_geometry(fegpu_femm *femm, int sdim, const double *xyz);
+/* IntegDomain(fes, rule, axisymmetric = true) (src/IntegDomainModule.jl:43-143):
+ * a two-manifold measured as a volume is scaled by 2 pi r at each point (r:
+ * the point's first coordinate, src/IntegDomainModule.jl:521-549) instead of
+ * the other dimension.  Default 0. */
+int fegpu_femm_set_axisymmetric(fegpu_femm *femm, int axisymmetric);
 /* element colours (1-based, element order) and their count. */
 int fegpu_femm_colors(fegpu_femm *femm, int64_t *colors, int64_t *ncolors);
 

@@ -870,13 +870,20 @@ static const double *coef_at(const orc_coef *c, int64_t e, int q, int npts) {
   return c->data + ((size_t)e * npts + q) * c->ncomp;
 }
 
+static const double kPi = 3.14159265358979323846; /* Julia's pi as Float64 */
+
 /* Jacobianmdim / Jacobianvolume (src/IntegDomainModule.jl:370-383, 405-450,
  * 504-549, 567-602): a two-manifold integrated as a volume, and a curve
- * integrated as a surface or a volume, are scaled by the other dimension. */
-static double jac_mdim(const orc_problem *p, int mdim, const double *J, int m) {
+ * integrated as a surface or a volume, are scaled by the other dimension;
+ * on an axisymmetric domain by 2 pi r instead (r = loc[0]), a curve
+ * integrated as a volume by both. */
+static double jac_mdim(const orc_problem *p, int mdim, const double *J, const double *loc,
+                       int m) {
   double d = jac_det(p->sdim, mdim, J);
-  if (mdim == 2 && m == 3) return d * p->otherdim;
-  if (mdim == 1 && m >= 2) return d * p->otherdim;
+  if (mdim == 2 && m == 3) return p->axisymmetric ? d * 2 * kPi * loc[0] : d * p->otherdim;
+  if (mdim == 1 && m == 2) return p->axisymmetric ? d * 2 * kPi * loc[0] : d * p->otherdim;
+  if (mdim == 1 && m == 3)
+    return p->axisymmetric ? d * 2 * kPi * loc[0] * p->otherdim : d * p->otherdim;
   return d;
 }
 
@@ -942,7 +949,7 @@ orc_matrix *orc_bilform(const orc_problem *p, int form, const orc_coef *c, int m
       locjac(nne, sdim, mdim, X, N, dN, loc, J);
       const double *cv = coef_at(c, e, q, npts);
       if (form == ORC_DIFFUSION) {
-        double Jac = jac_mdim(p, mdim, J, 3);
+        double Jac = jac_mdim(p, mdim, J, loc, 3);
         if (iso) {
           grad_n(nne, mdim, dN, J, g); /* the iso form ignores the frame */
           /* add_mggt_ut_only! (src/MatrixUtilityModule.jl:84-98) */
@@ -972,7 +979,7 @@ orc_matrix *orc_bilform(const orc_problem *p, int form, const orc_coef *c, int m
             }
         }
       } else if (form == ORC_LIN_ELASTIC) {
-        double Jac = jac_mdim(p, mdim, J, 3);
+        double Jac = jac_mdim(p, mdim, J, loc, 3);
         /* src/FEMMBaseModule.jl:1801-1804: RmTJ = Rm' J, blmat! with Rm */
         grad_n(nne, mdim, dN, rmtj(p, mdim, J, RmTJ), g);
         blmat3d(nne, g, p->rm, B);
@@ -992,7 +999,7 @@ orc_matrix *orc_bilform(const orc_problem *p, int form, const orc_coef *c, int m
           }
       } else if (form == ORC_DIV_GRAD) {
         /* bilform_div_grad, src/FEMMBaseModule.jl:1690-1710 (full matrix) */
-        double Jac = jac_mdim(p, mdim, J, 3);
+        double Jac = jac_mdim(p, mdim, J, loc, 3);
         grad_n(nne, mdim, dN, J, g);
         double factor = cv[0] * (Jac * p->w[q]);
         for (int aa = 0; aa < nne; ++aa)
@@ -1007,7 +1014,7 @@ orc_matrix *orc_bilform(const orc_problem *p, int form, const orc_coef *c, int m
               }
             }
       } else { /* ORC_DOT, src/FEMMBaseModule.jl:1348-1364 */
-        double Jac = jac_mdim(p, mdim, J, m);
+        double Jac = jac_mdim(p, mdim, J, loc, m);
         for (int k = 0; k < nne; ++k)
           for (int mm = 0; mm < nne; ++mm) {
             double factor = N[k] * N[mm] * Jac * p->w[q];
@@ -1070,7 +1077,7 @@ orc_matrix *orc_bilform_convection(const orc_problem *p, const double *vel, int 
     for (int q = 0; q < npts; ++q) {
       const double *N = Ns + q * nne, *dN = dNs + q * nne * mdim;
       locjac(nne, sdim, mdim, X, N, dN, loc, J);
-      double Jac = jac_mdim(p, mdim, J, 3);
+      double Jac = jac_mdim(p, mdim, J, loc, 3);
       grad_n(nne, mdim, dN, J, g);
       for (int pp = 0; pp < nne; ++pp)
         for (int r = 0; r < nne; ++r) {
@@ -1127,7 +1134,7 @@ orc_matrix *orc_bilform_masslike(const orc_problem *p, const orc_coef *c, int m)
     for (int q = 0; q < npts; ++q) {
       const double *N = Ns + q * nne, *dN = dNs + q * nne * mdim;
       locjac(nne, sdim, mdim, X, N, dN, loc, J);
-      double Jac = jac_mdim(p, mdim, J, m);
+      double Jac = jac_mdim(p, mdim, J, loc, m);
       const double *cv = coef_at(c, e, q, npts);
       for (int b = 0; b < nne; ++b) {
         double factor = N[b] * Jac * p->w[q];
@@ -1174,7 +1181,7 @@ int orc_linform_dot(const orc_problem *p, const orc_coef *f, int m, double *F) {
     for (int q = 0; q < npts; ++q) {
       const double *N = Ns + q * nne, *dN = dNs + q * nne * mdim;
       locjac(nne, sdim, mdim, X, N, dN, loc, J);
-      double Jac = jac_mdim(p, mdim, J, m);
+      double Jac = jac_mdim(p, mdim, J, loc, m);
       const double *force = coef_at(f, e, q, npts);
       double Factor = Jac * p->w[q];
       int rx = 0;

@@ -53,6 +53,7 @@ typedef struct {
   double otherdim;        /* constant "other dimension" (thickness)         */
   const double *rm;       /* material frame: constant 3x3 rotation matrix,  */
                           /* row-major (CSys csmat), or NULL = identity     */
+  int axisymmetric;       /* IntegDomain(..., axisymmetric = true)          */
 } orc_problem;
 
 typedef struct {

@@ -43,7 +43,7 @@ class _Problem(C.Structure):
         ("nnodes", C.c_int64), ("sdim", C.c_int), ("xyz", C.c_void_p),
         ("ndn", C.c_int), ("dofnums", C.c_void_p), ("nalldofs", C.c_int64),
         ("npts", C.c_int), ("pc", C.c_void_p), ("w", C.c_void_p),
-        ("otherdim", C.c_double), ("rm", C.c_void_p),
+        ("otherdim", C.c_double), ("rm", C.c_void_p), ("axisymmetric", C.c_int),
     ]
 
 
@@ -268,7 +268,8 @@ class Assembler:
             self.h = None
 
 
-def _problem(etype, conn, xyz, dofnums, nalldofs, pc, w, otherdim, keep, rm=None):
+def _problem(etype, conn, xyz, dofnums, nalldofs, pc, w, otherdim, keep, rm=None,
+             axisymmetric=False):
     conn = np.ascontiguousarray(conn, dtype=np.int64)
     xyz = np.ascontiguousarray(xyz, dtype=np.float64)
     dofnums = np.ascontiguousarray(dofnums, dtype=np.int64)
@@ -284,7 +285,7 @@ def _problem(etype, conn, xyz, dofnums, nalldofs, pc, w, otherdim, keep, rm=None
         rmp = _p(rm)
     return _Problem(etype, conn.shape[0], _p(conn), xyz.shape[0], xyz.shape[1], _p(xyz),
                     dofnums.shape[1], _p(dofnums), int(nalldofs), len(w), _p(pc), _p(w),
-                    float(otherdim), rmp)
+                    float(otherdim), rmp, int(bool(axisymmetric)))
 
 
 def _coef(kind, data, keep):
@@ -301,14 +302,15 @@ def _coef(kind, data, keep):
 
 
 def bilform(form, etype, conn, xyz, dofnums, nalldofs, pc, w, coef, coef_kind=COEF_CONST,
-            otherdim=1.0, m=3, symmetric=True, phases=False, asm=None, rm=None):
+            otherdim=1.0, m=3, symmetric=True, phases=False, asm=None, rm=None,
+            axisymmetric=False):
     """One bilinear form, assembled like the reference's 4/5-argument call.
 
     Returns the scipy CSC matrix (and, optionally, the number of exact zeros
     dropped by the symmetric completion and the phase timings).
     """
     keep = []
-    P = _problem(etype, conn, xyz, dofnums, nalldofs, pc, w, otherdim, keep, rm)
+    P = _problem(etype, conn, xyz, dofnums, nalldofs, pc, w, otherdim, keep, rm, axisymmetric)
     Cf = _coef(coef_kind, coef, keep)
     ph = np.zeros(3)
     kind = asm if asm is not None else (ASM_SPARSE_SYMM if symmetric else ASM_SPARSE)
@@ -319,11 +321,13 @@ def bilform(form, etype, conn, xyz, dofnums, nalldofs, pc, w, coef, coef_kind=CO
     return K
 
 
-def bilform_convection(etype, conn, xyz, dofnums, nalldofs, pc, w, velocity, otherdim=1.0):
+def bilform_convection(etype, conn, xyz, dofnums, nalldofs, pc, w, velocity, otherdim=1.0,
+                       axisymmetric=False):
     """bilform_convection (scalar field) with SysmatAssemblerSparse; velocity
     nnodes x nsd."""
     keep = []
-    P = _problem(etype, conn, xyz, dofnums, nalldofs, pc, w, otherdim, keep)
+    P = _problem(etype, conn, xyz, dofnums, nalldofs, pc, w, otherdim, keep,
+                 axisymmetric=axisymmetric)
     v = np.ascontiguousarray(velocity, dtype=np.float64)
     h = lib().orc_bilform_convection(C.byref(P), _p(v), v.shape[1])
     K, _ = _take_matrix(h)
@@ -331,21 +335,23 @@ def bilform_convection(etype, conn, xyz, dofnums, nalldofs, pc, w, velocity, oth
 
 
 def bilform_masslike(etype, conn, xyz, dofnums, nalldofs, pc, w, coef, coef_kind=COEF_CONST,
-                     otherdim=1.0, m=3):
+                     otherdim=1.0, m=3, axisymmetric=False):
     """bilform_masslike with SysmatAssemblerSparse: the nelem*ndn x nalldofs
     matrix whose rows (i-1)*ndn+1 .. i*ndn belong to element i; coef ndn x ndn
     (constant, per element or per quadrature point)."""
     keep = []
-    P = _problem(etype, conn, xyz, dofnums, nalldofs, pc, w, otherdim, keep)
+    P = _problem(etype, conn, xyz, dofnums, nalldofs, pc, w, otherdim, keep,
+                 axisymmetric=axisymmetric)
     Cf = _coef(coef_kind, coef, keep)
     K, _ = _take_matrix(lib().orc_bilform_masslike(C.byref(P), C.byref(Cf), m))
     return K
 
 
 def linform_dot(etype, conn, xyz, dofnums, nalldofs, pc, w, force, coef_kind=COEF_CONST,
-                otherdim=1.0, m=3):
+                otherdim=1.0, m=3, axisymmetric=False):
     keep = []
-    P = _problem(etype, conn, xyz, dofnums, nalldofs, pc, w, otherdim, keep)
+    P = _problem(etype, conn, xyz, dofnums, nalldofs, pc, w, otherdim, keep,
+                 axisymmetric=axisymmetric)
     Cf = _coef(coef_kind, force, keep)
     F = np.zeros(int(nalldofs))
     if lib().orc_linform_dot(C.byref(P), C.byref(Cf), m, _p(F)) != 0:

@@ -289,6 +289,18 @@ def ffblock_case():
             "tol": 1.0e-5}
 
 
+def axisymmetric_case():
+    """Volume of an axisymmetric domain (test/test_basics.jl, module
+    mbas010x1): the rectangle a x b revolved about the axis has volume
+    pi a^2 b."""
+    rel = "test/test_basics.jl"
+    txt, line = module_text(read(rel), "mbas010x1", rel)
+    a, b, na, nb = tuple_vals(txt, "a, b, na, nb")
+    order = int(re.search(r"GaussRule\(2,\s*(\d+)\)", txt).group(1))
+    return {"source": f"{rel}:{line}", "a": a, "b": b, "na": int(na), "nb": int(nb),
+            "gauss_order": order}
+
+
 def masslike_case():
     """bilform_masslike known answer (test/test_forms.jl, module
     mbilform_masslike_1): the L2 mesh's node coordinates, the Gauss order and
@@ -308,7 +320,8 @@ def main():
         sys.exit(f"reference sources not found at {REF}")
     data = {"assembler": assembler_kats(), "patch": patch_tests(), **coloring_and_pattern(),
             "conjugategradient": cg_case(), "masslike": masslike_case(),
-            "div_grad": div_grad_cases(), "ffblock": ffblock_case()}
+            "div_grad": div_grad_cases(), "ffblock": ffblock_case(),
+            "axisymmetric": axisymmetric_case()}
     with open(OUT, "w") as f:
         json.dump(data, f, indent=1)
     print("wrote", OUT)

@@ -998,3 +998,91 @@ def test_rule_too_large_is_refused(ft):
     with pytest.raises(ft.FegpuError, match="too large"):
         ft.bilform_lin_elastic(femm, ft.NodalField(fens.xyz), u, ft.DeforModelRed3D,
                                ft.DataCache(ft.isotropic_D(1.0, 0.3)))
+
+
+def _axisym_case(ft, kats, jitter=True):
+    k = kats["axisymmetric"]
+    fens, fes = ft.Q4block(k["a"], k["b"], k["na"] + 3, k["nb"] + 2)
+    if jitter:
+        fens.xyz = ft.meshes.jitter_interior(fens.xyz, (k["na"] + 3, k["nb"] + 2), 0.15, 9,
+                                             box=(k["a"], k["b"]))
+    femm = ft.FEMMBase(ft.IntegDomain(fes, ft.GaussRule(2, k["gauss_order"]), True))
+    return k, fens, fes, femm, ft.NodalField(fens.xyz)
+
+
+def test_axisymmetric_volume(ft, kats):
+    """test/test_basics.jl mbas010x1 through the GPU forms: the rectangle
+    revolved about the axis has volume pi a^2 b (1' M 1 of bilform_dot with
+    m = 3), FP64 and mixed; m = 2 measures the area."""
+    k, fens, fes, femm, geom = _axisym_case(ft, kats, jitter=False)
+    u = _field(ft, fens.count(), 1)
+    one = np.ones(fens.count())
+    V = np.pi * k["a"] ** 2 * k["b"]
+    for prec in ("fp64", "mixed"):
+        M = ft.bilform_dot(femm, ft.SysmatAssemblerGPU(precision=prec), geom, u,
+                           ft.DataCache(np.eye(1)), m=3)
+        assert abs(one @ M @ one - V) <= (1e-12 if prec == "fp64" else 1e-6) * V
+    S = ft.bilform_dot(femm, geom, u, ft.DataCache(np.eye(1)), m=2)
+    assert abs(one @ S @ one - k["a"] * k["b"]) <= 1e-12 * k["a"] * k["b"]
+
+
+@pytest.mark.parametrize("form", ["dot", "diffusion", "diffusion_general", "linform", "lumped",
+                                  "masslike", "convection"])
+def test_axisymmetric_forms(ft, O, kats, form):
+    """Axisymmetric Q4 domains (2 pi r in place of the other dimension) for
+    every form that measures a two-manifold as a volume, against the oracle;
+    the mixed path within the mixed bound."""
+    k, fens, fes, femm, geom = _axisym_case(ft, kats)
+    npts, Ns, dN, w, pc = femm.integdomain.integrationdata()
+    n = fens.count()
+    kw = dict(otherdim=1.0, axisymmetric=True)
+    if form == "dot":
+        u = _field(ft, n, 3)
+        c = np.diag([1.0, 2.0, 3.0])
+        K = ft.bilform_dot(femm, geom, u, ft.DataCache(c), m=3)
+        Kr = O.bilform(O.DOT, fes.code, fes.conn, geom.values, u.dofnums, u.nalldofs(), pc, w, c,
+                       m=3, **kw)
+        K32 = ft.bilform_dot(femm, ft.SysmatAssemblerGPU(precision="mixed"), geom, u,
+                             ft.DataCache(c), m=3)
+    elif form in ("diffusion", "diffusion_general"):
+        u = _field(ft, n, 1)
+        c = 1.7 if form == "diffusion" else np.array([[2.0, 0.3], [0.3, 1.0]])
+        K = ft.bilform_diffusion(femm, geom, u, ft.DataCache(c))
+        Kr = O.bilform(O.DIFFUSION, fes.code, fes.conn, geom.values, u.dofnums, u.nalldofs(),
+                       pc, w, np.atleast_1d(c), **kw)
+        K32 = ft.bilform_diffusion(femm, ft.SysmatAssemblerGPU(precision="mixed"), geom, u,
+                                   ft.DataCache(c))
+    elif form == "linform":
+        u = _field(ft, n, 2)
+        f = np.array([1.0, -0.5])
+        F = ft.linform_dot(femm, geom, u, ft.DataCache(f), 3)
+        Fr = O.linform_dot(fes.code, fes.conn, geom.values, u.dofnums, u.nalldofs(), pc, w, f,
+                           m=3, **kw)
+        assert np.allclose(F, Fr, rtol=1e-12, atol=1e-14 * np.abs(Fr).max())
+        return
+    elif form == "lumped":
+        u = _field(ft, n, 1)
+        K = ft.bilform_dot(femm, ft.SysmatAssemblerSparseHRZLumpingSymmGPU(), geom, u,
+                           ft.DataCache(np.eye(1) * 7.0), m=3)
+        Kr = O.bilform(O.DOT, fes.code, fes.conn, geom.values, u.dofnums, u.nalldofs(), pc, w,
+                       np.eye(1) * 7.0, m=3, asm=O.ASM_HRZ, **kw)
+        compare(K, Kr)
+        return
+    elif form == "masslike":
+        u = _field(ft, n, 1)
+        K = ft.bilform_masslike(femm, geom, u, ft.DataCache(np.eye(1) * 2.0))
+        Kr = O.bilform_masslike(fes.code, fes.conn, geom.values, u.dofnums, u.nalldofs(), pc, w,
+                                np.eye(1) * 2.0, **kw)
+        compare(K, Kr)
+        return
+    else:
+        q = _field(ft, n, 1)
+        vel = ft.NodalField(np.column_stack([np.full(n, 0.7), np.full(n, -1.1)]))
+        K = ft.bilform_convection(femm, geom, vel, q, ft.DataCache(1.0))
+        Kr = O.bilform_convection(fes.code, fes.conn, geom.values, q.dofnums, q.nalldofs(), pc,
+                                  w, vel.values, **kw)
+        compare(K, Kr)
+        return
+    compare(K, Kr)
+    x = np.random.default_rng(5).uniform(-1, 1, K.shape[0])
+    assert np.linalg.norm((K32 - K) @ x) <= MIXED_TOL * np.linalg.norm(K @ x)

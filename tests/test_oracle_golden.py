@@ -321,3 +321,24 @@ def test_kat_div_grad(O, kats, idx):
         G2 = O.bilform(O.LIN_ELASTIC, et, conn, xyz, dofs, 3 * n, pc, w, C)
         e1, e2 = v @ G @ v, v @ G2 @ v
         assert abs(e1 - e2) / e1 <= tol
+
+
+def test_kat_axisymmetric_volume(O, kats):
+    """test/test_basics.jl mbas010x1: the a x b rectangle revolved about the
+    axis has volume pi a^2 b (there integrated on Q8; here the same identity
+    through bilform_dot on Q4 of an axisymmetric domain: 1' M 1 = volume,
+    exact for the rule since 2 pi r is linear)."""
+    k = kats["axisymmetric"]
+    xyz, conn = O.q4blockx(O.linearspace(0.0, k["a"], k["na"] + 1),
+                           O.linearspace(0.0, k["b"], k["nb"] + 1))
+    n = xyz.shape[0]
+    pc, w = O.gauss_rule(2, k["gauss_order"])
+    M = O.bilform(O.DOT, O.Q4, conn, xyz, np.arange(1, n + 1), n, pc, w, np.eye(1),
+                  m=3, axisymmetric=True)
+    one = np.ones(n)
+    V = np.pi * k["a"] ** 2 * k["b"]
+    assert abs(one @ M @ one - V) <= 1e-12 * V
+    # the surface measure (m = 2) ignores the axisymmetry: the area a b
+    S = O.bilform(O.DOT, O.Q4, conn, xyz, np.arange(1, n + 1), n, pc, w, np.eye(1),
+                  m=2, axisymmetric=True)
+    assert abs(one @ S @ one - k["a"] * k["b"]) <= 1e-12 * k["a"] * k["b"]
