@@ -99,7 +99,9 @@ int choose_tile(int etype, int form, int precision, int npts) {
   return te;
 }
 
-int mixed_tile_for(int etype, int form, int npts) { return default_tile(etype, form, npts); }
+int mixed_tile_for(int etype, int form, int npts, bool wide) {
+  return default_tile(etype, form, npts, wide);
+}
 size_t mixed_smem_for(int etype, int form, int npts, int te) {
   return tile_smem_bytes(etype, form, npts, te);
 }
@@ -302,7 +304,7 @@ void run_gather(fegpu_dofmap *dm, int form, KArgs &a) {
   const int bs = ndn * ndn, nblk = nne * (nne + 1) / 2;
   if (!dm->gather_ready) build_gather_plan(dm, nblk * bs);
   a.conn = fm->conn_orig.as<int32_t>();
-  a.te = default_tile(fm->etype, form, fm->npts);
+  a.te = default_tile(fm->etype, form, fm->npts, false);  // the single-call tile
   FEGPU_REQUIRE(tile_smem_bytes(fm->etype, form, fm->npts, a.te) <= 227 * 1024,
                 "quadrature rule too large for the element kernel");
   GArgs g;

@@ -247,7 +247,8 @@ int launch_gather(int etype, int ndn, const GArgs &g, int num_sms, cudaStream_t 
 int launch_gather_inline_slot(int etype, int ndn, const GArgs &g, int num_sms, cudaStream_t s);
 int launch_mixed(int etype, int form, const KArgs &a, int sms, cudaStream_t s);
 // elements per tile and the tile's shared memory for a form of the mixed path
-int mixed_tile_for(int etype, int form, int npts);
+// elements per mixed tile: wide = the persistent batch kernel's tile shape
+int mixed_tile_for(int etype, int form, int npts, bool wide = true);
 size_t mixed_smem_for(int etype, int form, int npts, int te);
 
 // Node coordinates: column-major nnodes x sdim (device) -> [nnodes][4] (device).

@@ -22,10 +22,14 @@
 
 namespace fegpu {
 
-// node pairs per tile: 2 a's x 4 b's for H20, 2 x 2 otherwise
-template <int NNE> struct FastTiles {
+// node pairs per tile: 2 a's x 2 b's, or 2 x 4 for H20 in the persistent
+// batch kernel (WIDE): there the CTA count is fixed at two per SM and the
+// wider tile's register reuse pays (256-mesh batch 90 ms against 95 ms),
+// while the single-call kernel runs faster with more, narrower CTAs (H20
+// 40^3: 1.69 ms against 1.78 ms per mixed assembly)
+template <int NNE, bool WIDE = true> struct FastTiles {
   static constexpr int TA = 2;
-  static constexpr int TB = NNE >= 20 ? 4 : 2;
+  static constexpr int TB = (WIDE && NNE >= 20) ? 4 : 2;
   static constexpr int NA = (NNE + TA - 1) / TA;
   static constexpr int NB = (NNE + TB - 1) / TB;
   // tiles (A, B) holding at least one pair with b >= a, B fastest
@@ -75,16 +79,16 @@ __host__ __device__ inline FastLayout fast_layout(int nne, int npts, int te, int
 }
 
 // elements per tile: enough (element, tile) tasks for 256 threads
-__host__ __device__ constexpr int fast_tiles_for(int nne) {
-  return nne >= 20 ? FastTiles<20>::NT
+__host__ __device__ constexpr int fast_tiles_for(int nne, bool wide = true) {
+  return nne >= 20 ? (wide ? FastTiles<20, true>::NT : FastTiles<20, false>::NT)
                    : (nne >= 10 ? FastTiles<10>::NT : (nne >= 8 ? FastTiles<8>::NT : FastTiles<4>::NT));
 }
 // the largest tile: one (element, node-pair tile) task per thread
-inline int max_fast_tile(int etype) {
-  const int nt = fast_tiles_for(nodes_per_elem(etype));
+inline int max_fast_tile(int etype, bool wide = true) {
+  const int nt = fast_tiles_for(nodes_per_elem(etype), wide);
   return std::max(1, kMixedThreads / nt);
 }
-inline int default_fast_tile(int etype) { return max_fast_tile(etype); }
+inline int default_fast_tile(int etype, bool wide = true) { return max_fast_tile(etype, wide); }
 
 // Phases A, B and B' of the tile (shared with the tensor-core tile of
 // mixed_tc.cuh): connectivity and Lame pairs, FP32 coordinates relative to the
@@ -231,7 +235,7 @@ __device__ __forceinline__ void fast_geometry(const KArgs &a, int64_t eb, int ne
   __syncthreads();
 }
 
-template <int ET, int FORM, int NDN>
+template <int ET, int FORM, int NDN, bool WIDE = true>
 __device__ __forceinline__ void mixed_tile_fast(const KArgs &a, int64_t eb, int ne,
                                                 unsigned char *smem, float *ke, int64_t e0) {
   constexpr int NNE = ElemT<ET>::NNE, MDIM = ElemT<ET>::MDIM;
@@ -239,7 +243,7 @@ __device__ __forceinline__ void mixed_tile_fast(const KArgs &a, int64_t eb, int 
   constexpr int BS = NDN * NDN;
   constexpr bool GRAD = FORM != F_DOT;
   constexpr int SLOTS = fast_stride(NNE);
-  using T = FastTiles<NNE>;
+  using T = FastTiles<NNE, WIDE>;
   constexpr int TA = T::TA, TB = T::TB, NT = T::NT;
   static_assert(FORM == F_DIFF_ISO || FORM == F_ELAST_ISO || FORM == F_DOT, "isotropic forms");
   const int npts = a.npts, te = a.te;
@@ -460,9 +464,9 @@ inline size_t tile_smem_bytes(int etype, int form, int npts, int te) {
 
 // elements per tile; rules with many points (Gauss orders above 3) get fewer
 // elements so that a tile's tables stay within a CTA's shared memory
-inline int default_tile(int etype, int form, int npts) {
+inline int default_tile(int etype, int form, int npts, bool wide = true) {
   int te = (form == F_DIFF_ISO || form == F_ELAST_ISO || form == F_DOT)
-               ? default_fast_tile(etype)
+               ? default_fast_tile(etype, wide)
                : default_general_tile(etype, npts);
   while (te > 1 && tile_smem_bytes(etype, form, npts, te) > 200 * 1024) --te;
   return te;
@@ -476,7 +480,7 @@ __global__ void __launch_bounds__(kMixedThreads) k_blocks_mixed(const KArgs a) {
   for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const int64_t eb = a.e0 + tile * a.te;
     const int ne = static_cast<int>(min(static_cast<int64_t>(a.te), a.e1 - eb));
-    if constexpr (kFastForm<FORM>) mixed_tile_fast<ET, FORM, NDN>(a, eb, ne, smem, a.ke, a.e0);
+    if constexpr (kFastForm<FORM>) mixed_tile_fast<ET, FORM, NDN, false>(a, eb, ne, smem, a.ke, a.e0);
     else mixed_tile<ET, FORM, NDN>(a, eb, ne, smem, a.ke, a.e0);
   }
 }
@@ -484,7 +488,8 @@ __global__ void __launch_bounds__(kMixedThreads) k_blocks_mixed(const KArgs a) {
 template <int ET, int FORM, int NDN>
 int launch_blocks_mixed_t(const KArgs &a, int num_sms, cudaStream_t s) {
   if constexpr (kFastForm<FORM>)
-    FEGPU_REQUIRE(a.te >= 1 && a.te <= max_fast_tile(ET), "mixed: elements per tile out of range");
+    FEGPU_REQUIRE(a.te >= 1 && a.te <= max_fast_tile(ET, false),
+                  "mixed: elements per tile out of range");
   const size_t smem = tile_smem_bytes(ET, FORM, a.npts, a.te);
   auto kern = k_blocks_mixed<ET, FORM, NDN>;
   FEGPU_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -182,7 +182,7 @@ extern "C" int fegpu_bilform_lin_elastic_noalloc(fegpu_matrix *K, const fegpu_co
     }
 
     a.conn = fm->conn_orig.as<int32_t>();
-    a.te = mixed_tile_for(fm->etype, form, fm->npts);
+    a.te = mixed_tile_for(fm->etype, form, fm->npts, false);  // the single-call tile
     FEGPU_REQUIRE(mixed_smem_for(fm->etype, form, fm->npts, a.te) <= 227 * 1024,
                   "quadrature rule too large for the element kernel");
     GArgs g;
