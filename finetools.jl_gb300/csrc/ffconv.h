@@ -1,11 +1,12 @@
-// Float-float (h + l, two FP32 words) to FP64 with integer arithmetic only:
-// the mixed path's final conversion of each CSR value.  GB300's FP64 pipe
-// (and its FP32 <-> FP64 conversions) runs at a small fraction of the integer
-// and FP32 rates, so the conversion works on the bit patterns.  The file is
+// Float-float (h + l, two FP32 words) to FP64 without the FP64 pipe: the
+// mixed path's final conversion of each CSR value.  GB300's FP64 pipe (and
+// its FP32 <-> FP64 conversions) runs at a small fraction of the integer and
+// FP32 rates, so the conversion works on the bit patterns.  The file is
 // also compiled by the host compiler (tests/ffconv_check.cpp checks both
 // routines against exact rational arithmetic).
 #pragma once
 
+#include <cmath>
 #include <cstdint>
 #include <cstring>
 
@@ -50,6 +51,30 @@ FEGPU_HD inline float fsub(float a, float b) {
   return __fsub_rn(a, b);
 #else
   return a - b;
+#endif
+}
+FEGPU_HD inline float ffrom(uint32_t u) {
+#if defined(__CUDA_ARCH__)
+  return __uint_as_float(u);
+#else
+  float f;
+  std::memcpy(&f, &u, 4);
+  return f;
+#endif
+}
+FEGPU_HD inline float fmul(float a, float b) {
+#if defined(__CUDA_ARCH__)
+  return __fmul_rn(a, b);
+#else
+  return a * b;
+#endif
+}
+// nearest integer, ties to even (|x| < 2^31)
+FEGPU_HD inline int32_t f2i_rn(float x) {
+#if defined(__CUDA_ARCH__)
+  return __float2int_rn(x);
+#else
+  return static_cast<int32_t>(std::nearbyint(x));  // default rounding mode
 #endif
 }
 FEGPU_HD inline int clz64(uint64_t x) {
@@ -131,33 +156,33 @@ FEGPU_HD inline FEGPU_NOINLINE double ff_to_double_exact(float h, float l) {
                (mant & ((1ull << 52) - 1ull)));
 }
 
-// (h + l) as FP64, faithfully (error below one unit in the last place), in
-// about 25 integer operations for the common case: after renormalisation l
-// is at least 24 binades below h (d = e_h - e_l >= 24), so h's 24-bit
-// mantissa fills the top of the FP64 mantissa, whose low 29 bits are free,
-// and l adds or subtracts c = m_l * 2^(29 - d) < 2^29 units of the last place
-// (bits of l below the last place truncated).  An addition cannot carry out
-// of the free bits; a subtraction borrows across h's binade only when h's
-// mantissa is zero.  Other inputs (zero, subnormal, inf/nan, d < 24, that
-// borrow) take ff_to_double_exact.
+// (h + l) rounded to FP64 (nearest, ties to even) in about 20 integer
+// operations, one FP32 multiply and one float-to-integer conversion for the
+// common case.  After renormalisation |l| <= ulp_32(h) / 2, so the exact sum
+// is h's FP64 image (24-bit mantissa at the top of the 52-bit field, low 29
+// bits zero) plus c_f units of its last place, c_f = l * 2^(179 - e_h),
+// |c_f| <= 2^28.  The scaling by a power of two (carrying h's sign, so that a
+// positive c_f grows the magnitude) is exact; rounding c_f to the nearest
+// integer (ties to even: the parity of the result's last bit is c's) and
+// adding it to the bit pattern rounds the sum once.  An addition cannot carry
+// out of the free bits; when h is a power of two and l lowers its magnitude
+// the sum lies in the binade below, whose units are half as large: c_f is
+// then taken at twice the scale and the borrow lands on the right pattern.
+// Other inputs (zero, subnormal or tiny h with e_h < 53, inf/nan) take
+// ff_to_double_exact.
 FEGPU_HD inline double ff_to_double(float h0, float l0) {
   using namespace ffconv;
   float h = h0, l = l0;
   renormalise(h, l);
   const uint32_t hb = fbits(h), lb = fbits(l);
-  const uint32_t eh = (hb >> 23) & 0xffu, el = (lb >> 23) & 0xffu;
-  const uint32_t mh = hb & 0x7fffffu;
-  const int d = static_cast<int>(eh) - static_cast<int>(el);
-  if (eh == 0u || eh == 0xffu || (el != 0u && d < 24)) return ff_to_double_exact(h0, l0);
-  const bool same = ((hb ^ lb) >> 31) == 0u;
-  uint32_t c = 0u;
-  if (el != 0u) {
-    const uint32_t ml = (lb & 0x7fffffu) | 0x800000u;
-    c = d <= 29 ? (ml << (29 - d)) : (d < 61 ? (ml >> (d - 29)) : 0u);
-  }
-  if (c != 0u && !same && mh == 0u) return ff_to_double_exact(h0, l0);
-  uint64_t D = (static_cast<uint64_t>(eh + 896u) << 52) | (static_cast<uint64_t>(mh) << 29);
-  D = same ? (D | c) : (D - c);
+  const uint32_t eh = (hb >> 23) & 0xffu;
+  if (eh - 53u > 201u) return ff_to_double_exact(h0, l0);
+  const uint32_t down = ((hb & 0x7fffffu) == 0u && ((hb ^ lb) >> 31) != 0u) ? 1u : 0u;
+  const float scale = ffrom(((306u - eh + down) << 23) | (hb & 0x80000000u));
+  const int32_t c = f2i_rn(fmul(l, scale));
+  const uint64_t mag = (static_cast<uint64_t>(((hb & 0x7fffffffu) >> 3) + (896u << 20)) << 32) |
+                       static_cast<uint64_t>(hb << 29);
+  const uint64_t D = mag + static_cast<uint64_t>(static_cast<int64_t>(c));
   return dfrom(D | (static_cast<uint64_t>(hb >> 31) << 63));
 }
 

@@ -1,5 +1,6 @@
 // Row gather of the mixed-precision path: per-node accumulation of element
-// blocks with compensated FP32 sums and integer-only rounding to FP64.
+// blocks with compensated FP32 sums, rounded once to FP64 on the integer and
+// FP32 pipes.
 // Shared by the single-matrix gather kernel (gather.cu) and the batch kernel
 // (batch.cu).
 #pragma once

@@ -5,9 +5,9 @@ arithmetic on ~44,000 pairs (tests/ffconv_check.cpp):
     l's bits reach at most 37 binades below h (else within one half unit plus
     the truncated part); zero / FP32-subnormal sums give signed zeros; inf
     and nan keep their class;
-  - ff_to_double (the row gather's routine): within one unit in the last
-    place of h + l (faithful) for every finite normal case, and equal to the
-    exact routine on the special cases.
+  - ff_to_double (the row gather's routine): the same bound (nearest FP64,
+    ties to even) for every finite case, and equal to the exact routine on
+    the special cases.
 No GPU is involved.
 """
 import os
@@ -64,8 +64,10 @@ def test_float_float_to_double(tmp_path):
         # exact routine: within half an ulp (plus the bits it truncates)
         err_ex = abs(Fraction(ex) - exact)
         assert err_ex <= _ulp(ex) / 2 + abs(exact) * Fraction(2) ** -60, line
-        # gather routine: faithful
+        # gather routine: nearest, ties to even
         err_fa = abs(Fraction(fa) - exact)
-        assert err_fa < _ulp(fa), line
+        assert err_fa <= _ulp(fa) / 2 + abs(exact) * Fraction(2) ** -60, line
+        if err_fa == _ulp(fa) / 2:
+            assert struct.unpack(">Q", struct.pack(">d", fa))[0] % 2 == 0, line
         n_checked += 1
     assert n_checked > 40000
