@@ -12,12 +12,19 @@ is also provided, for element matrices computed by the caller.
 from __future__ import annotations
 
 import ctypes as C
+import itertools
 import weakref
 
 import numpy as np
 import scipy.sparse as sp
 
 from . import _native as nat
+
+
+# per-assembler keys of the device matrices a DOF map holds (an object's id
+# can be reused once it is freed, which would hand a new assembler the matrix
+# of an earlier device result)
+_assembler_serial = itertools.count()
 
 
 def _is_assembler(x) -> bool:
@@ -124,6 +131,7 @@ class SysmatAssemblerGPU:
         self._generic_fin = None
         self._shape = None
         self._nomatrixresult = False
+        self._key = ("assembler", next(_assembler_serial))
 
     def eltype(self):
         return np.float64
@@ -135,7 +143,10 @@ class SysmatAssemblerGPU:
 
     # ---- device forms --------------------------------------------------------
     def _matrix_for(self, dm):
-        key = id(self)
+        """The device matrix this assembler fills on the DOF map dm: one per
+        (assembler, DOF map), so a device result stays valid until the same
+        assembler assembles again on the same DOF map."""
+        key = self._key
         h = dm.matrices.get(key)
         if h is None:
             out = C.c_void_p()

@@ -382,6 +382,24 @@ def test_determinism(ft):
     assert np.array_equal(v1, v2)
 
 
+def test_device_results_do_not_alias(ft):
+    """A device result keeps its values while other (short-lived) assemblers
+    assemble on the same mesh: each assembler fills its own device matrix,
+    whatever object ids the interpreter reuses."""
+    fens, fes = ft.h8_diffusion_mesh(n=4, seed=3)
+    femm = ft.FEMMBase(ft.IntegDomain(fes, ft.GaussRule(3, 2)))
+    geom = ft.NodalField(fens.xyz)
+    u = _field(ft, fens.count(), 1)
+    K1 = ft.bilform_diffusion(femm, ft.SysmatAssemblerGPU(result="device"), geom, u,
+                              ft.DataCache(1.0))
+    v1 = K1.values().copy()
+    for prec in ("fp64", "mixed", "fp64", "mixed"):
+        K2 = ft.bilform_diffusion(femm, ft.SysmatAssemblerGPU(precision=prec, result="device"),
+                                  geom, u, ft.DataCache(2.0))
+        assert np.abs(K2.values() - 2.0 * v1).max() <= 1e-6 * np.abs(v1).max()
+    assert np.array_equal(K1.values(), v1)
+
+
 def test_colouring_matches_reference(ft, O, kats):
     k = kats["coloring_t4"]
     fens, fes = ft.T4block(*k["block"])

@@ -118,3 +118,12 @@ def test_vector_blocked(ft):
     assert ft.vector_blocked_f(v, 0).size == 0 and ft.vector_blocked_d(v, 7).size == 0
     with pytest.raises(ValueError, match="too many rows"):
         ft.vector_blocked_f(v, 8)
+
+
+def test_assembler_matrix_keys_unique(ft):
+    """Device matrices are keyed per assembler by a serial number, never by
+    an object id that a freed assembler leaves for the next one."""
+    keys = set()
+    for _ in range(200):
+        keys.add(ft.SysmatAssemblerGPU()._key)  # each assembler freed at once
+    assert len(keys) == 200
