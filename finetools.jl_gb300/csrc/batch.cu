@@ -49,10 +49,9 @@ template <int NNE, int NDN>
 __device__ void batch_gather(const GArgs &g, int64_t b, int64_t e, unsigned char *smem) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int wstride = gather_warp_stride(NDN, g.maxdeg);
-  float *hi = reinterpret_cast<float *>(smem) + static_cast<size_t>(warp) * wstride;
-  float *lo = hi + NDN * g.maxdeg * NDN;
+  float *acc = reinterpret_cast<float *>(smem) + static_cast<size_t>(warp) * wstride;
   for (int64_t t = b + warp; t < e; t += kGatherWarps)
-    gather_node<NNE, NDN, false, true>(g, g.nodes[t], hi, lo, lane);
+    gather_node<NNE, NDN, false, true>(g, g.nodes[t], acc, lane);
 }
 
 __device__ void elem_dispatch(const BatchJob &J, int64_t b, int64_t e, int64_t chunk,

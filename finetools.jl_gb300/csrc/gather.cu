@@ -29,11 +29,10 @@ __global__ void __launch_bounds__(kGatherWarps * 32) k_gather(const GArgs g) {
   // per-warp region padded to a multiple of 4 floats: every warp's region
   // starts on a 16-byte boundary (the zeroing stores float4)
   const int wstride = gather_warp_stride(NDN, g.maxdeg);
-  float *hi = gsm + static_cast<size_t>(warp) * wstride;
-  float *lo = hi + NDN * g.maxdeg * NDN;
+  float *acc = gsm + static_cast<size_t>(warp) * wstride;
   for (int64_t t = g.n0 + static_cast<int64_t>(blockIdx.x) * kGatherWarps + warp; t < g.n1;
        t += static_cast<int64_t>(gridDim.x) * kGatherWarps)
-    gather_node<NNE, NDN, INLINE_SLOT>(g, g.nodes[t], hi, lo, lane);
+    gather_node<NNE, NDN, INLINE_SLOT>(g, g.nodes[t], acc, lane);
 }
 
 template <int NNE, int NDN, bool INLINE_SLOT = false>

@@ -32,27 +32,78 @@ __device__ __forceinline__ void two_sum_acc(float &h, float &l, float v) {
   l = __fadd_rn(l, err);
 }
 
-// One warp gathers the rows of node A: accumulators hi/lo (NDN x cmax floats
-// each, in the warp's shared region), blocks of the incident elements in
+// a - b rounded once, on a register pair (fma(b, -1, a) is exact up to the
+// one rounding, like __fsub_rn)
+__device__ __forceinline__ float2 fsub2(float2 a, float2 b) {
+  return __ffma2_rn(b, make_float2(-1.f, -1.f), a);
+}
+// two_sum_acc on two independent accumulators at once (paired FP32
+// instructions; the same operations per component)
+__device__ __forceinline__ void two_sum_acc2(float2 &h, float2 &l, float2 v) {
+  const float2 s = __fadd2_rn(h, v);
+  const float2 bb = fsub2(s, h);
+  const float2 err = __fadd2_rn(fsub2(h, fsub2(s, bb)), fsub2(v, bb));
+  h = s;
+  l = __fadd2_rn(l, err);
+}
+
+// The accumulators of column c of a node's rows: NDN = 3 keeps rows 0 and 1
+// as one float4 (h0, h1, l0, l1) in a01[c] and row 2 as (h2, l2) in a2[c];
+// NDN = 1 keeps (h, l) in a2[c].  Same size as NDN (hi, lo) float pairs.
+template <int NDN> struct GatherAcc {
+  float4 *a01;
+  float2 *a2;
+  __device__ __forceinline__ GatherAcc(float *base, int cmax)
+      : a01(reinterpret_cast<float4 *>(base)),
+        a2(reinterpret_cast<float2 *>(base + (NDN == 3 ? 4 * cmax : 0))) {}
+  __device__ __forceinline__ void add(int c, const float (&v)[NDN]) const {
+    if constexpr (NDN == 3) {
+      float4 a = a01[c];
+      float2 h = make_float2(a.x, a.y), l = make_float2(a.z, a.w);
+      two_sum_acc2(h, l, make_float2(v[0], v[1]));
+      a01[c] = make_float4(h.x, h.y, l.x, l.y);
+    }
+    float2 b = a2[c];
+    two_sum_acc(b.x, b.y, v[NDN - 1]);
+    a2[c] = b;
+  }
+  // (h, l) of row i at column c
+  __device__ __forceinline__ void get(int c, float (&h)[NDN], float (&l)[NDN]) const {
+    if constexpr (NDN == 3) {
+      const float4 a = a01[c];
+      h[0] = a.x;
+      h[1] = a.y;
+      l[0] = a.z;
+      l[1] = a.w;
+    }
+    const float2 b = a2[c];
+    h[NDN - 1] = b.x;
+    l[NDN - 1] = b.y;
+  }
+};
+
+// One warp gathers the rows of node A: accumulators (GatherAcc, 2 NDN cmax
+// floats in the warp's shared region), blocks of the incident elements in
 // element order, then one FP64 store per CSR value of the node's rows.
 // L2ONLY reads the blocks with ld.global.cg (no L1 allocation): required when
 // the blocks were written earlier in the same launch by other CTAs.  PIPE
 // loads element k + 1's block entries before accumulating element k (more
 // registers: the persistent batch kernel, capped at 128, keeps the plain loop).
 template <int NNE, int NDN, bool INLINE_SLOT, bool L2ONLY = false, bool PIPE = !L2ONLY>
-__device__ __forceinline__ void gather_node(const GArgs &g, int32_t A, float *hi, float *lo,
-                                            int lane) {
+__device__ __forceinline__ void gather_node(const GArgs &g, int32_t A, float *accbase, int lane) {
+  static_assert(NDN == 1 || NDN == 3, "the mixed path gathers 1 or 3 DOFs per node");
   constexpr int NBLK = NNE * (NNE + 1) / 2;
   constexpr int BS = NDN * NDN;
   constexpr int NTASK = NNE * NDN;  // (b, j): node of the element, column component
   constexpr int NSLOT = (NTASK + 31) / 32;
   const int cmax = g.maxdeg * NDN;
   const int cols = static_cast<int>(g.nptr[A + 1] - g.nptr[A]) * NDN;
+  const GatherAcc<NDN> acc(accbase, cmax);
   {
-    float4 *z = reinterpret_cast<float4 *>(hi);  // hi and lo are contiguous
+    float4 *z = reinterpret_cast<float4 *>(accbase);
     const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
     for (int c = lane; c < (2 * NDN * cmax) / 4; c += 32) z[c] = zero;
-    for (int c = ((2 * NDN * cmax) / 4) * 4 + lane; c < 2 * NDN * cmax; c += 32) hi[c] = 0.f;
+    for (int c = ((2 * NDN * cmax) / 4) * 4 + lane; c < 2 * NDN * cmax; c += 32) accbase[c] = 0.f;
   }
   // the lane's (b, j) tasks, fixed for all incident elements
   int tb[NSLOT], tj[NSLOT], trow[NSLOT];
@@ -116,9 +167,7 @@ __device__ __forceinline__ void gather_node(const GArgs &g, int32_t A, float *hi
 #pragma unroll
       for (int s2 = 0; s2 < NSLOT; ++s2) {
         if (lane + 32 * s2 >= NTASK) break;
-#pragma unroll
-        for (int i = 0; i < NDN; ++i)
-          two_sum_acc(hi[i * cmax + cc[s2]], lo[i * cmax + cc[s2]], vc[s2][i]);
+        acc.add(cc[s2], vc[s2]);
       }
       __syncwarp();
 #pragma unroll
@@ -156,19 +205,20 @@ __device__ __forceinline__ void gather_node(const GArgs &g, int32_t A, float *hi
       float v[NDN];
 #pragma unroll
       for (int i = 0; i < NDN; ++i) v[i] = L2ONLY ? __ldcg(blk + i * step) : blk[i * step];
-#pragma unroll
-      for (int i = 0; i < NDN; ++i) two_sum_acc(hi[i * cmax + col], lo[i * cmax + col], v[i]);
+      acc.add(col, v);
     }
     __syncwarp();
   }
   }
+  int64_t base[NDN];
 #pragma unroll
-  for (int i = 0; i < NDN; ++i) {
-    const int64_t base = g.rowptr[g.dof[A * NDN + i]];
-    for (int c = lane; c < cols; c += 32) {
-      const int64_t off = g.colperm ? g.colperm[g.cpoff[A] * NDN + c] : c;
-      g.val[base + off] = ff_to_double(hi[i * cmax + c], lo[i * cmax + c]);
-    }
+  for (int i = 0; i < NDN; ++i) base[i] = g.rowptr[g.dof[A * NDN + i]];
+  for (int c = lane; c < cols; c += 32) {
+    const int64_t off = g.colperm ? g.colperm[g.cpoff[A] * NDN + c] : c;
+    float h[NDN], l[NDN];
+    acc.get(c, h, l);
+#pragma unroll
+    for (int i = 0; i < NDN; ++i) g.val[base[i] + off] = ff_to_double(h[i], l[i]);
   }
   __syncwarp();
 }
