@@ -32,6 +32,9 @@ template <int NNE, bool WIDE = true> struct FastTiles {
   static constexpr int TB = (WIDE && NNE >= 20) ? 4 : 2;
   static constexpr int NA = (NNE + TA - 1) / TA;
   static constexpr int NB = (NNE + TB - 1) / TB;
+  // the first tile of row A holding a pair with b >= a:
+  // TB B + TB - 1 >= TA A  <=>  B >= floor(TA A / TB)
+  __host__ __device__ static constexpr int bmin(int A) { return (TA * A) / TB; }
   // tiles (A, B) holding at least one pair with b >= a, B fastest
   static constexpr int count() {
     int n = 0;
@@ -293,15 +296,25 @@ __device__ __forceinline__ void mixed_tile_fast(const KArgs &a, int64_t eb, int 
     const int i = tid;
     const bool active = i < ne * NT;
     const int e = active ? i / NT : 0;
+    // task t -> tile (A, B), row after row with B fastest: a loop over the
+    // rows (row A holds the tiles B >= bmin(A)) for the long tile lists
+    // (H20: 55 tiles), an unrolled search for the short ones
     int t = active ? i - e * NT : 0, A = 0, B = 0;
-    {
+    if constexpr (NT > 16) {
+      for (; A < T::NA - 1; ++A) {
+        const int len = T::NB - T::bmin(A);
+        if (t < len) break;
+        t -= len;
+      }
+      B = T::bmin(A) + t;
+    } else {
       int n = 0;
       bool found = false;
 #pragma unroll
       for (int AA = 0; AA < T::NA; ++AA)
 #pragma unroll
         for (int BB = 0; BB < T::NB; ++BB)
-          if (TB * BB + TB - 1 >= TA * AA) {
+          if (BB >= T::bmin(AA)) {
             if (!found && n == t) {
               A = AA;
               B = BB;
@@ -472,16 +485,29 @@ inline int default_tile(int etype, int form, int npts, bool wide = true) {
   return te;
 }
 
+// the register-tiled forms, held to 64 registers: four CTAs per SM
 template <int ET, int FORM, int NDN>
-__global__ void __launch_bounds__(kMixedThreads) k_blocks_mixed(const KArgs a) {
+__global__ void __launch_bounds__(kMixedThreads, 4) k_blocks_mixed(const KArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int64_t nel = a.e1 - a.e0;
   const int64_t ntiles = (nel + a.te - 1) / a.te;
   for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const int64_t eb = a.e0 + tile * a.te;
     const int ne = static_cast<int>(min(static_cast<int64_t>(a.te), a.e1 - eb));
-    if constexpr (kFastForm<FORM>) mixed_tile_fast<ET, FORM, NDN, false>(a, eb, ne, smem, a.ke, a.e0);
-    else mixed_tile<ET, FORM, NDN>(a, eb, ne, smem, a.ke, a.e0);
+    mixed_tile_fast<ET, FORM, NDN, false>(a, eb, ne, smem, a.ke, a.e0);
+  }
+}
+
+// general conductivity / general D (the tile of mixed.cuh)
+template <int ET, int FORM, int NDN>
+__global__ void __launch_bounds__(kMixedThreads) k_blocks_mixed_general(const KArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int64_t nel = a.e1 - a.e0;
+  const int64_t ntiles = (nel + a.te - 1) / a.te;
+  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int64_t eb = a.e0 + tile * a.te;
+    const int ne = static_cast<int>(min(static_cast<int64_t>(a.te), a.e1 - eb));
+    mixed_tile<ET, FORM, NDN>(a, eb, ne, smem, a.ke, a.e0);
   }
 }
 
@@ -491,7 +517,9 @@ int launch_blocks_mixed_t(const KArgs &a, int num_sms, cudaStream_t s) {
     FEGPU_REQUIRE(a.te >= 1 && a.te <= max_fast_tile(ET, false),
                   "mixed: elements per tile out of range");
   const size_t smem = tile_smem_bytes(ET, FORM, a.npts, a.te);
-  auto kern = k_blocks_mixed<ET, FORM, NDN>;
+  void (*kern)(const KArgs);
+  if constexpr (kFastForm<FORM>) kern = k_blocks_mixed<ET, FORM, NDN>;
+  else kern = k_blocks_mixed_general<ET, FORM, NDN>;
   FEGPU_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   static_cast<int>(smem)));
   int per_sm = 0;
