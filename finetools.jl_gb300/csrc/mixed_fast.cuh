@@ -86,10 +86,15 @@ __host__ __device__ constexpr int fast_tiles_for(int nne, bool wide = true) {
   return nne >= 20 ? (wide ? FastTiles<20, true>::NT : FastTiles<20, false>::NT)
                    : (nne >= 10 ? FastTiles<10>::NT : (nne >= 8 ? FastTiles<8>::NT : FastTiles<4>::NT));
 }
+// threads of a CTA of the single-call element-block kernel: 128 (eight CTAs
+// per SM at 64 registers), so that a barrier between the tile's phases holds
+// four warps, not eight; the persistent batch kernel keeps kMixedThreads
+constexpr int kFastThreads = 128;
+
 // the largest tile: one (element, node-pair tile) task per thread
 inline int max_fast_tile(int etype, bool wide = true) {
   const int nt = fast_tiles_for(nodes_per_elem(etype), wide);
-  return std::max(1, kMixedThreads / nt);
+  return std::max(1, (wide ? kMixedThreads : kFastThreads) / nt);
 }
 inline int default_fast_tile(int etype, bool wide = true) { return max_fast_tile(etype, wide); }
 
@@ -485,9 +490,9 @@ inline int default_tile(int etype, int form, int npts, bool wide = true) {
   return te;
 }
 
-// the register-tiled forms, held to 64 registers: four CTAs per SM
+// the register-tiled forms, held to 64 registers: eight CTAs per SM
 template <int ET, int FORM, int NDN>
-__global__ void __launch_bounds__(kMixedThreads, 4) k_blocks_mixed(const KArgs a) {
+__global__ void __launch_bounds__(kFastThreads, 8) k_blocks_mixed(const KArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int64_t nel = a.e1 - a.e0;
   const int64_t ntiles = (nel + a.te - 1) / a.te;
@@ -522,14 +527,15 @@ int launch_blocks_mixed_t(const KArgs &a, int num_sms, cudaStream_t s) {
   else kern = k_blocks_mixed_general<ET, FORM, NDN>;
   FEGPU_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   static_cast<int>(smem)));
+  const int threads = kFastForm<FORM> ? kFastThreads : kMixedThreads;
   int per_sm = 0;
-  FEGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kMixedThreads, smem));
+  FEGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem));
   per_sm = std::max(per_sm, 1);
   const int64_t nel = a.e1 - a.e0;
   if (nel <= 0) return 0;
   const int64_t ntiles = (nel + a.te - 1) / a.te;
   const int grid = static_cast<int>(std::min<int64_t>(ntiles, static_cast<int64_t>(num_sms) * per_sm));
-  kern<<<grid, kMixedThreads, smem, s>>>(a);
+  kern<<<grid, threads, smem, s>>>(a);
   FEGPU_CUDA(cudaGetLastError());
   return 1;
 }
