@@ -234,10 +234,16 @@ KArgs base_args(fegpu_matrix *K, fegpu_dofmap *dm) {
   // error from 1.2e-6 to 1.4e-7 (max |dK| / max |K|) for 17 % more time.
   // FEGPU_MIXED_FP64_GEOMETRY=1 / 0 forces FP64 geometry for every / only the
   // distorted elements of any type.
-  a.distort_tol = fm->etype == FEGPU_T10 ? 2.0 : 0.1;
+  // FP64 geometry in the mixed tiles: distorted elements (det_min / det_max
+  // below 0.1) and curved T10 (an isoparametric T10 Jacobian entry sums ten
+  // cancelling terms; a straight-sided T10 is affine and takes its exact
+  // corner Jacobian in FP32).  FEGPU_MIXED_FP64_GEOMETRY=1: FP64 for every
+  // element; =0: only for the distorted ones (isoparametric FP32 T10).
+  a.distort_tol = 0.1;
+  a.t10_affine = fm->etype == FEGPU_T10 ? 1 : 0;
   if (const char *env = std::getenv("FEGPU_MIXED_FP64_GEOMETRY")) {
     if (env[0] == '1') a.distort_tol = 2.0;
-    else if (env[0] == '0') a.distort_tol = 0.1;
+    else if (env[0] == '0') a.t10_affine = 0;
   }
   return a;
 }

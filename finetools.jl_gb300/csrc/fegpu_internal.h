@@ -202,6 +202,8 @@ struct KArgs {
   double otherdim;
   int axisym;              // axisymmetric domain: 2 pi r instead of otherdim
   double distort_tol;      // mixed path: det_min/det_max below -> FP64 geometry
+  int t10_affine;          // mixed path, T10: straight-sided elements take the FP32
+                           // corner Jacobian, curved ones FP64 geometry
   int64_t e0, e1;          // colour range of sorted elements
   int *status;             // device status word (0 = ok)
   float *ke;               // block-output mode: element blocks of elements e0.. (or null)

@@ -71,6 +71,24 @@ __host__ __device__ constexpr int mixed_groups(int nne) {
 }
 
 // FP64 Jacobian, determinant and inverse of one point (distorted elements).
+// det J and J^-1 (row-major) of a 3 x 3 Jacobian by cofactors, in FP64
+__device__ __forceinline__ void inverse3_fp64(const double (&J)[3][3], double *inv, double &det) {
+  const double c0 = J[1][1] * J[2][2] - J[2][1] * J[1][2];
+  const double c1 = J[1][0] * J[2][2] - J[1][2] * J[2][0];
+  const double c2 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+  det = J[0][0] * c0 - J[0][1] * c1 + J[0][2] * c2;
+  const double id = 1.0 / det;
+  inv[0] = c0 * id;
+  inv[1] = -(J[0][1] * J[2][2] - J[0][2] * J[2][1]) * id;
+  inv[2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
+  inv[3] = -c1 * id;
+  inv[4] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
+  inv[5] = -(J[0][0] * J[1][2] - J[1][0] * J[0][2]) * id;
+  inv[6] = (J[1][0] * J[2][1] - J[2][0] * J[1][1]) * id;
+  inv[7] = -(J[0][0] * J[2][1] - J[2][0] * J[0][1]) * id;
+  inv[8] = (J[0][0] * J[1][1] - J[1][0] * J[0][1]) * id;
+}
+
 template <int NNE, int MDIM>
 __device__ void jacobian_fp64(const double *xyz, const int32_t *conn, const double *dN, int sdim,
                               double *inv, double &det) {
@@ -89,20 +107,7 @@ __device__ void jacobian_fp64(const double *xyz, const int32_t *conn, const doub
     }
   }
   if constexpr (MDIM == 3) {
-    const double c0 = J[1][1] * J[2][2] - J[2][1] * J[1][2];
-    const double c1 = J[1][0] * J[2][2] - J[1][2] * J[2][0];
-    const double c2 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
-    det = J[0][0] * c0 - J[0][1] * c1 + J[0][2] * c2;
-    const double id = 1.0 / det;
-    inv[0] = c0 * id;
-    inv[1] = -(J[0][1] * J[2][2] - J[0][2] * J[2][1]) * id;
-    inv[2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
-    inv[3] = -c1 * id;
-    inv[4] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
-    inv[5] = -(J[0][0] * J[1][2] - J[1][0] * J[0][2]) * id;
-    inv[6] = (J[1][0] * J[2][1] - J[2][0] * J[1][1]) * id;
-    inv[7] = -(J[0][0] * J[2][1] - J[2][0] * J[0][1]) * id;
-    inv[8] = (J[0][0] * J[1][1] - J[1][0] * J[0][1]) * id;
+    inverse3_fp64(J, inv, det);
   } else {
     det = J[0][0] * J[1][1] - J[1][0] * J[0][1];
     const double id = 1.0 / det;
@@ -242,7 +247,9 @@ __device__ __forceinline__ void mixed_tile(const KArgs &a, int64_t eb, int ne,
         dmax = fmaxf(dmax, v);
       }
       float det = sDet[i];
-      if (GRAD && !(dmin > tol * dmax)) {
+      // T10 under the affine policy: FP64 geometry for every element here
+      // (this tile does not test for straight sides)
+      if (GRAD && (!(dmin > tol * dmax) || (NNE == 10 && a.t10_affine))) {
         double inv[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, dd;
         jacobian_fp64<NNE, MDIM>(a.xyz, sConn + e * NNE, tabdN + q * NNE * MDIM, a.sdim, inv, dd);
 #pragma unroll

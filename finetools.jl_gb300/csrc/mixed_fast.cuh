@@ -131,12 +131,32 @@ __device__ __forceinline__ void fast_geometry(const KArgs &a, int64_t eb, int ne
     }
   }
   __syncthreads();
-  // A. FP32 coordinates relative to the first node
+  // A. FP32 coordinates relative to the first node.  T10 (affine policy): the
+  // w slot of a mid-edge node holds 1 when the node is off its edge's
+  // midpoint by more than 2^-30 of the edge (FP64 test), else 0
+  constexpr bool T10 = (NNE == 10 && MDIM == 3);
   for (int i = tid; i < ne * NNE; i += nth) {
-    const int e = i / NNE;
+    const int e = i / NNE, k = i - e * NNE;
     const double *p = a.xyz + 4 * static_cast<int64_t>(sConn[i]);
     const double *p0 = a.xyz + 4 * static_cast<int64_t>(sConn[e * NNE]);
-    fX[i] = make_float4(float(p[0] - p0[0]), float(p[1] - p0[1]), float(p[2] - p0[2]), 0.f);
+    float curved = 0.f;
+    if constexpr (T10) {
+      if (a.t10_affine && k >= 4) {
+        // edges of the mid-edge nodes 4..9: (0,1) (1,2) (2,0) (3,0) (3,1) (3,2)
+        const int ea = k < 7 ? k - 4 : 3;
+        const int eb = k < 7 ? (k == 6 ? 0 : k - 3) : k - 7;
+        const double *pa = a.xyz + 4 * static_cast<int64_t>(sConn[e * NNE + ea]);
+        const double *pb = a.xyz + 4 * static_cast<int64_t>(sConn[e * NNE + eb]);
+        double dev = 0.0, len = 0.0;
+#pragma unroll
+        for (int s = 0; s < 3; ++s) {
+          dev = fmax(dev, fabs(p[s] - 0.5 * (pa[s] + pb[s])));
+          len = fmax(len, fabs(pb[s] - pa[s]));
+        }
+        curved = dev > 0x1p-30 * len ? 1.f : 0.f;
+      }
+    }
+    fX[i] = make_float4(float(p[0] - p0[0]), float(p[1] - p0[1]), float(p[2] - p0[2]), curved);
   }
   __syncthreads();
   // B. J, det J, J^-1 per (element, point)
@@ -145,6 +165,34 @@ __device__ __forceinline__ void fast_geometry(const KArgs &a, int64_t eb, int ne
     const float4 *X = fX + e * NNE;
     const float *d = fdN + q * NNE * MDIM;
     float J[3][MDIM];
+    if constexpr (T10 && GRAD) {
+      bool affine = a.t10_affine != 0;
+#pragma unroll
+      for (int k = 4; k < 10; ++k) affine = affine && X[k].w == 0.f;
+      if (affine) {
+        // straight-sided T10: x = X0 + r (X1 - X0) + s (X2 - X0) + t (X3 - X0),
+        // J constant; formed once per element in FP64 from the corners (the
+        // point-0 thread) and rounded to FP32 for every point
+        if (q == 0) {
+          const int32_t *ce = sConn + e * NNE;
+          const double *p0 = a.xyz + 4 * static_cast<int64_t>(ce[0]);
+          double Jd[3][3], invd[9], detd;
+#pragma unroll
+          for (int m = 0; m < 3; ++m) {
+            const double *pm = a.xyz + 4 * static_cast<int64_t>(ce[m + 1]);
+#pragma unroll
+            for (int s = 0; s < 3; ++s) Jd[s][m] = pm[s] - p0[s];
+          }
+          inverse3_fp64(Jd, invd, detd);
+          for (int qq = 0; qq < npts; ++qq) {
+#pragma unroll
+            for (int r = 0; r < 9; ++r) sJinv[(i + qq) * 9 + r] = float(invd[r]);
+            sDet[i + qq] = float(detd);
+          }
+        }
+        continue;
+      }
+    }
 #pragma unroll
     for (int s = 0; s < 3; ++s)
 #pragma unroll
@@ -212,7 +260,14 @@ __device__ __forceinline__ void fast_geometry(const KArgs &a, int64_t eb, int ne
         dmin = fminf(dmin, v);
         dmax = fmaxf(dmax, v);
       }
-      if (!(dmin > tol * dmax)) {
+      bool curved = false;
+      if constexpr (T10) {
+        if (a.t10_affine) {
+#pragma unroll
+          for (int k = 4; k < 10; ++k) curved = curved || fX[e * NNE + k].w != 0.f;
+        }
+      }
+      if (curved || !(dmin > tol * dmax)) {
         double inv[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, dd;
         jacobian_fp64<NNE, MDIM>(a.xyz, sConn + e * NNE, tabdN + q * NNE * MDIM, a.sdim, inv, dd);
 #pragma unroll

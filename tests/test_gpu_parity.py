@@ -594,6 +594,36 @@ def test_mixed_precision(ft, O, et):
     assert abs(K32 - K32.T).max() == 0.0
 
 
+@pytest.mark.parametrize("curved", [False, True])
+def test_mixed_t10_straight_and_curved(ft, curved):
+    """Mixed T10 elasticity within the mixed bound of FP64 on straight-sided
+    elements (affine: the FP32 corner Jacobian) and on elements whose
+    mid-edge nodes are moved off the edges (curved: FP64 geometry), and on a
+    mesh that mixes both."""
+    fens, fes = ft.t10_elastic_mesh(n=5, seed=9)
+    xyz = fens.xyz.copy()
+    if curved:
+        rng = np.random.default_rng(12)
+        mids = np.unique(fes.conn[:, 4:].ravel() - 1)
+        pick = mids[rng.random(mids.size) < 0.5]  # about half the mid-edge nodes
+        interior = np.all((xyz[pick] > 1e-9) & (xyz[pick] < 1 - 1e-9), axis=1)
+        pick = pick[interior]
+        xyz[pick] += rng.uniform(-0.02, 0.02, (pick.size, 3)) / 5
+    femm = ft.FEMMBase(ft.IntegDomain(fes, ft.TetRule(4)))
+    geom = ft.NodalField(xyz)
+    u = _field(ft, fens.count(), 3)
+    rng = np.random.default_rng(5)
+    cf = ft.IsotropicElementwise(rng.lognormal(np.log(70e9), 0.5, fes.count()),
+                                 rng.uniform(0.2, 0.35, fes.count()))
+    K64 = ft.bilform_lin_elastic(femm, ft.SysmatAssemblerGPU(), geom, u, ft.DeforModelRed3D, cf)
+    K32 = ft.bilform_lin_elastic(femm, ft.SysmatAssemblerGPU(precision="mixed"), geom, u,
+                                 ft.DeforModelRed3D, cf)
+    x = rng.uniform(-1, 1, K64.shape[0])
+    assert np.linalg.norm((K32 - K64) @ x) / np.linalg.norm(K64 @ x) <= MIXED_TOL
+    assert abs(K32 - K64).max() / abs(K64).max() <= MIXED_TOL
+    assert abs(K32 - K32.T).max() == 0.0
+
+
 # ---------------------------------------------------------------- masslike
 def _masslike_case(ft, et, seed=17):
     rng = np.random.default_rng(seed)
