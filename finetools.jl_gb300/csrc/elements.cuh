@@ -46,7 +46,7 @@ template <> struct ElemT<FEGPU_T4> { static constexpr int NNE = 4, MDIM = 3; };
 template <> struct ElemT<FEGPU_T10> { static constexpr int NNE = 10, MDIM = 3; };
 
 struct SmemLayout {
-  size_t tab, X, G, WG, Jw, det, conn, pairs, total;
+  size_t tab, X, G, WG, Jw, det, aff, conn, pairs, total;
 };
 
 __host__ __device__ inline size_t align_up(size_t o, size_t a) { return (o + a - 1) / a * a; }
@@ -72,6 +72,11 @@ __host__ __device__ inline SmemLayout smem_layout(int nne, int mdim, int npts, i
   o = align_up(o, 16);
   L.det = o;
   o += sizeof(float) * te * npts;
+  o = align_up(o, 16);
+  // T10 gradient forms: per node, 1 when a mid-edge node is off its edge's
+  // midpoint
+  L.aff = o;
+  if (grad && nne == 10 && mdim == 3) o += sizeof(uint8_t) * te * nne;
   o = align_up(o, 16);
   L.conn = o;
   o += sizeof(int32_t) * te * nne;
@@ -116,6 +121,43 @@ __device__ __forceinline__ C madd(C a, C b, C c) {  // c + a*b
   else return fma(a, b, c);
 }
 
+// det J (returned) and, with INV, J^-1 of a 3 x 3 Jacobian by cofactors
+// (Jacobian(), src/FESetModule.jl:426-435; gradN!, 507-544).
+template <typename C, bool EX, bool INV>
+__device__ __forceinline__ C det_inverse3(const C (&J)[3][3], C (&inv)[3][3]) {
+  const C c0 = sub<C, EX>(mul<C, EX>(J[1][1], J[2][2]), mul<C, EX>(J[2][1], J[1][2]));
+  const C c1 = sub<C, EX>(mul<C, EX>(J[1][0], J[2][2]), mul<C, EX>(J[1][2], J[2][0]));
+  const C c2 = sub<C, EX>(mul<C, EX>(J[1][0], J[2][1]), mul<C, EX>(J[1][1], J[2][0]));
+  const C det = add<C, EX>(sub<C, EX>(mul<C, EX>(J[0][0], c0), mul<C, EX>(J[0][1], c1)), mul<C, EX>(J[0][2], c2));
+  if (INV) {
+    const C id = C(1) / det;
+    inv[0][0] = mul<C, EX>(c0, id);
+    inv[0][1] = mul<C, EX>(-sub<C, EX>(mul<C, EX>(J[0][1], J[2][2]), mul<C, EX>(J[0][2], J[2][1])), id);
+    inv[0][2] = mul<C, EX>(sub<C, EX>(mul<C, EX>(J[0][1], J[1][2]), mul<C, EX>(J[0][2], J[1][1])), id);
+    inv[1][0] = mul<C, EX>(-c1, id);
+    inv[1][1] = mul<C, EX>(sub<C, EX>(mul<C, EX>(J[0][0], J[2][2]), mul<C, EX>(J[0][2], J[2][0])), id);
+    inv[1][2] = mul<C, EX>(-sub<C, EX>(mul<C, EX>(J[0][0], J[1][2]), mul<C, EX>(J[1][0], J[0][2])), id);
+    inv[2][0] = mul<C, EX>(sub<C, EX>(mul<C, EX>(J[1][0], J[2][1]), mul<C, EX>(J[2][0], J[1][1])), id);
+    inv[2][1] = mul<C, EX>(-sub<C, EX>(mul<C, EX>(J[0][0], J[2][1]), mul<C, EX>(J[2][0], J[0][1])), id);
+    inv[2][2] = mul<C, EX>(sub<C, EX>(mul<C, EX>(J[0][0], J[1][1]), mul<C, EX>(J[1][0], J[0][1])), id);
+  }
+  return det;
+}
+
+// spatial gradients g_k = dN_k J^-1 (gradN!, src/FESetModule.jl:507-544)
+template <int NNE, int MDIM, typename C, typename T, bool EX, typename XT>
+__device__ __forceinline__ void gradients(const XT *dN, const C (&inv)[MDIM][MDIM], T *g) {
+#pragma unroll
+  for (int k = 0; k < NNE; ++k)
+#pragma unroll
+    for (int c = 0; c < MDIM; ++c) {
+      C v = mul<C, EX>(C(dN[k * MDIM]), inv[0][c]);
+#pragma unroll
+      for (int m = 1; m < MDIM; ++m) v = madd<C, EX>(C(dN[k * MDIM + m]), inv[m][c], v);
+      g[k * MDIM + c] = T(v);
+    }
+}
+
 // Geometry at one quadrature point, computed in C (double or float):
 // locjac! (J = X' dN, src/MatrixUtilityModule.jl:60-68), Jacobian()
 // (src/FESetModule.jl:426-435, 479-489) and gradN! (453-470, 507-544).
@@ -152,23 +194,7 @@ __device__ __forceinline__ C geometry_qp(const XT *X, const XT *dN, int sdim,
   C inv[MDIM][MDIM];
   C Jac;
   if constexpr (MDIM == 3) {
-    const C c0 = sub<C, EX>(mul<C, EX>(J[1][1], J[2][2]), mul<C, EX>(J[2][1], J[1][2]));
-    const C c1 = sub<C, EX>(mul<C, EX>(J[1][0], J[2][2]), mul<C, EX>(J[1][2], J[2][0]));
-    const C c2 = sub<C, EX>(mul<C, EX>(J[1][0], J[2][1]), mul<C, EX>(J[1][1], J[2][0]));
-    const C det = add<C, EX>(sub<C, EX>(mul<C, EX>(J[0][0], c0), mul<C, EX>(J[0][1], c1)), mul<C, EX>(J[0][2], c2));
-    Jac = det;
-    if (GRAD) {
-      const C id = C(1) / det;
-      inv[0][0] = mul<C, EX>(c0, id);
-      inv[0][1] = mul<C, EX>(-sub<C, EX>(mul<C, EX>(J[0][1], J[2][2]), mul<C, EX>(J[0][2], J[2][1])), id);
-      inv[0][2] = mul<C, EX>(sub<C, EX>(mul<C, EX>(J[0][1], J[1][2]), mul<C, EX>(J[0][2], J[1][1])), id);
-      inv[1][0] = mul<C, EX>(-c1, id);
-      inv[1][1] = mul<C, EX>(sub<C, EX>(mul<C, EX>(J[0][0], J[2][2]), mul<C, EX>(J[0][2], J[2][0])), id);
-      inv[1][2] = mul<C, EX>(-sub<C, EX>(mul<C, EX>(J[0][0], J[1][2]), mul<C, EX>(J[1][0], J[0][2])), id);
-      inv[2][0] = mul<C, EX>(sub<C, EX>(mul<C, EX>(J[1][0], J[2][1]), mul<C, EX>(J[2][0], J[1][1])), id);
-      inv[2][1] = mul<C, EX>(-sub<C, EX>(mul<C, EX>(J[0][0], J[2][1]), mul<C, EX>(J[2][0], J[0][1])), id);
-      inv[2][2] = mul<C, EX>(sub<C, EX>(mul<C, EX>(J[0][0], J[1][1]), mul<C, EX>(J[1][0], J[0][1])), id);
-    }
+    Jac = det_inverse3<C, EX, GRAD>(J, inv);
   } else {
     if (sdim == 2) {
       Jac = sub<C, EX>(mul<C, EX>(J[0][0], J[1][1]), mul<C, EX>(J[1][0], J[0][1]));
@@ -199,17 +225,7 @@ __device__ __forceinline__ C geometry_qp(const XT *X, const XT *dN, int sdim,
     }
   }
   if (det_out) *det_out = float(Jac);
-  if (GRAD) {
-#pragma unroll
-    for (int k = 0; k < NNE; ++k)
-#pragma unroll
-      for (int c = 0; c < MDIM; ++c) {
-        C v = mul<C, EX>(C(dN[k * MDIM]), inv[0][c]);
-#pragma unroll
-        for (int m = 1; m < MDIM; ++m) v = madd<C, EX>(C(dN[k * MDIM + m]), inv[m][c], v);
-        g[k * MDIM + c] = T(v);
-      }
-  }
+  if (GRAD) gradients<NNE, MDIM, C, T, EX>(dN, inv, g);
   return Jac;
 }
 
@@ -295,6 +311,10 @@ __global__ void __launch_bounds__(kFormThreads) k_form(const KArgs a) {
   float *sDet = reinterpret_cast<float *>(smem + L.det);
   int32_t *sConn = reinterpret_cast<int32_t *>(smem + L.conn);
   uint8_t *sPair = smem + L.pairs;
+  // straight-sided T10 in the elasticity forms: J constant (per node, 1 when
+  // the node is a mid-edge node off its edge's midpoint)
+  constexpr bool AFF = NNE == 10 && MDIM == 3 && (FORM == F_ELAST_ISO || FORM == F_ELAST_GEN);
+  uint8_t *sOff = smem + L.aff;
   const int tid = threadIdx.x, nth = blockDim.x;
 
   for (int i = tid; i < npts * NNE * (MDIM + 1) + npts; i += nth) {
@@ -324,6 +344,25 @@ __global__ void __launch_bounds__(kFormThreads) k_form(const KArgs a) {
       sX[3 * i] = p[0];
       sX[3 * i + 1] = p[1];
       sX[3 * i + 2] = p[2];
+      if constexpr (AFF) {
+        // a T10 whose mid-edge nodes are exactly (FP64) at their edge
+        // midpoints is the affine map x = X0 + r (X1 - X0) + s (X2 - X0) +
+        // t (X3 - X0): its isoparametric J (ten terms per point) is the
+        // constant [X1 - X0 | X2 - X0 | X3 - X0]
+        const int e = i / NNE, k = i - e * NNE;
+        uint8_t off = 0;
+        if (k >= 4) {
+          // edges of the mid-edge nodes 4..9: (0,1) (1,2) (2,0) (3,0) (3,1) (3,2)
+          const int ea = k < 7 ? k - 4 : 3;
+          const int eb = k < 7 ? (k == 6 ? 0 : k - 3) : k - 7;
+          const double *pa = a.xyz + 4 * static_cast<int64_t>(sConn[e * NNE + ea]);
+          const double *pb = a.xyz + 4 * static_cast<int64_t>(sConn[e * NNE + eb]);
+#pragma unroll
+          for (int c = 0; c < 3; ++c)
+            off |= p[c] != __dmul_rn(0.5, __dadd_rn(pa[c], pb[c])) ? 1 : 0;
+        }
+        sOff[i] = off;
+      }
     }
     __syncthreads();
 
@@ -332,6 +371,23 @@ __global__ void __launch_bounds__(kFormThreads) k_form(const KArgs a) {
       const int e = i / npts, q = i - e * npts;
       T *g = sG + (static_cast<size_t>(e) * npts + q) * NNE * MDIM;
       T *wg = sWG + (static_cast<size_t>(e) * npts + q) * NNE * MDIM;
+      if constexpr (AFF) {
+        const uint8_t *off = sOff + e * NNE;
+        if ((off[4] | off[5] | off[6] | off[7] | off[8] | off[9]) == 0) {
+          const double *X = sX + e * NNE * 3;
+          double J[3][3], inv[3][3];
+#pragma unroll
+          for (int c = 0; c < 3; ++c)
+#pragma unroll
+            for (int m = 0; m < 3; ++m) J[c][m] = X[3 * (m + 1) + c] - X[c];
+          const double det = det_inverse3<double, EXACT, true>(J, inv);
+          gradients<NNE, MDIM, double, T, EXACT>(sdN + q * NNE * MDIM, inv, g);
+          sDet[e * npts + q] = float(det);
+          qp_weights<NNE, MDIM, FORM, T>(a, eb + e, q, npts, T(det), sw[q], g, wg,
+                                         sJw + e * npts + q);
+          continue;
+        }
+      }
       const T Jac = geometry_qp<NNE, MDIM, GRAD, double, T, EXACT>(
           sX + e * NNE * 3, sdN + q * NNE * MDIM, a.sdim, vol, a.otherdim, g, sDet + e * npts + q,
           sN + q * NNE, a.axisym);
