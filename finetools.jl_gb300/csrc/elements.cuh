@@ -381,7 +381,37 @@ __global__ void __launch_bounds__(kFormThreads) k_form(const KArgs a) {
 #pragma unroll
             for (int m = 0; m < 3; ++m) J[c][m] = X[3 * (m + 1) + c] - X[c];
           const double det = det_inverse3<double, EXACT, true>(J, inv);
-          gradients<NNE, MDIM, double, T, EXACT>(sdN + q * NNE * MDIM, inv, g);
+          // gradients from the constant barycentric gradients: the rows of
+          // J^-1 are grad lambda_1..3, grad lambda_0 = -(their sum); the
+          // T10 basis gives g_k = (4 lambda_k - 1) grad lambda_k at a corner
+          // and 4 lambda_b grad lambda_a + 4 lambda_a grad lambda_b on edge
+          // (a, b); f_k = 4 lambda_k - 1 read from the caller's table (the
+          // parametric gradient of corner k is f_k d lambda_k)
+          const double *d = sdN + q * NNE * MDIM;
+          double gl[4][3], f[4];
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            gl[1][c] = inv[0][c];
+            gl[2][c] = inv[1][c];
+            gl[3][c] = inv[2][c];
+            gl[0][c] = -(inv[0][c] + inv[1][c] + inv[2][c]);
+          }
+          f[0] = -d[0];
+          f[1] = d[3];
+          f[2] = d[7];
+          f[3] = d[11];
+#pragma unroll
+          for (int k = 0; k < 4; ++k)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) g[k * 3 + c] = T(f[k] * gl[k][c]);
+#pragma unroll
+          for (int k = 4; k < 10; ++k) {
+            const int ea = k < 7 ? k - 4 : 3;
+            const int eb = k < 7 ? (k == 6 ? 0 : k - 3) : k - 7;
+            const double fa = f[ea] + 1.0, fb = f[eb] + 1.0;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) g[k * 3 + c] = T(fma(fb, gl[ea][c], fa * gl[eb][c]));
+          }
           sDet[e * npts + q] = float(det);
           qp_weights<NNE, MDIM, FORM, T>(a, eb + e, q, npts, T(det), sw[q], g, wg,
                                          sJw + e * npts + q);
