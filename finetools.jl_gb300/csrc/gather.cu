@@ -142,7 +142,9 @@ void build_gather_plan(fegpu_dofmap *dm, int block_values) {
   // ring: the chunks a gather reads (span + 1) plus one, so the element tiles
   // of the next chunk can be written while a gather still reads the ring
   dm->span = static_cast<int>(span);
-  dm->ring = static_cast<int>(std::min<int64_t>(span + 2, nch));
+  // (at least one slot: a mesh without elements has no chunk but keeps the
+  // per-slot events and slot arithmetic defined)
+  dm->ring = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(span + 2, nch)));
   for (size_t q = 0; q < elem.size(); ++q) {
     const int64_t ce = elem[q] / dm->chunk;
     slot[q] = static_cast<int32_t>((ce % dm->ring) * dm->chunk + (elem[q] - ce * dm->chunk));

@@ -21,8 +21,13 @@ MIXED_TOL = 1e-6
 
 
 def _rowmax(K):
+    """max |K_ij| per row (0 for an empty row)."""
     R = K.tocsr()
-    return np.maximum.reduceat(np.abs(R.data), R.indptr[:-1]) if R.nnz else np.zeros(0)
+    out = np.zeros(R.shape[0])
+    full = np.diff(R.indptr) > 0
+    if R.nnz:
+        out[full] = np.maximum.reduceat(np.abs(R.data), R.indptr[:-1][full])
+    return out
 
 
 RTOL = 1e-12
@@ -314,6 +319,60 @@ def test_general_dof_numbering_with_ebcs(ft, O):
                                ft.DeforModelRed3D, ft.DataCache(D))
     Kr = _oracle_form(O, femm, O.LIN_ELASTIC, geom, u, D, symmetric=False)
     compare(K, Kr)
+
+
+# ---------------------------------------------------------------- empty and ragged inputs
+def test_empty_element_set(ft):
+    """An element set without elements: every form returns the all-zero result
+    of the full size (FP64 and mixed), as makematrix! of an assembler that
+    received no triples does."""
+    fens, _ = ft.H8block(1.0, 1.0, 1.0, 2, 2, 2)
+    femm = ft.FEMMBase(ft.IntegDomain(ft.FESetH8(np.zeros((0, 8), dtype=np.int64)),
+                                      ft.GaussRule(3, 2)))
+    geom = ft.NodalField(fens.xyz)
+    u1 = _field(ft, fens.count(), 1)
+    u3 = _field(ft, fens.count(), 3)
+    for prec in ("fp64", "mixed"):
+        K = ft.bilform_diffusion(femm, ft.SysmatAssemblerGPU(precision=prec), geom, u1,
+                                 ft.DataCache(1.0))
+        assert K.shape == (u1.nalldofs(), u1.nalldofs()) and K.nnz == 0
+        K = ft.bilform_lin_elastic(femm, ft.SysmatAssemblerGPU(precision=prec), geom, u3,
+                                   ft.DeforModelRed3D, ft.DataCache(ft.isotropic_D(1.0, 0.3)))
+        assert K.shape == (u3.nalldofs(), u3.nalldofs()) and K.nnz == 0
+    F = ft.linform_dot(femm, geom, u3, ft.DataCache(np.array([1.0, 2.0, 3.0])), 3)
+    assert F.shape == (u3.nalldofs(),) and not F.any()
+
+
+def test_isolated_nodes_and_single_element(ft, O):
+    """Nodes that no element references, numbered among the others (their
+    rows and columns are empty), and a mesh of one element: FP64 against the
+    oracle, mixed against FP64."""
+    fens, fes = ft.H8block(1.0, 0.7, 0.5, 2, 2, 1)
+    rng = np.random.default_rng(8)
+    xyz = np.vstack([fens.xyz, rng.uniform(0, 1, (5, 3))])  # five nodes of no element
+    n = xyz.shape[0]
+    perm = rng.permutation(n)
+    where = np.empty(n, dtype=np.int64)
+    where[perm] = np.arange(n)
+    xyz = xyz[perm]
+    for conn in (where[fes.conn - 1] + 1, where[fes.conn[:1] - 1] + 1):
+        femm = ft.FEMMBase(ft.IntegDomain(ft.FESetH8(conn), ft.GaussRule(3, 2)))
+        geom = ft.NodalField(xyz)
+        u = _field(ft, n, 3)
+        D = ft.isotropic_D(1.0, 0.3)
+        # structural pattern (SysmatAssemblerSparse): the regular block has
+        # exact-zero couplings, which S + S' drops only when bitwise zero
+        K = ft.bilform_lin_elastic(femm, ft.SysmatAssemblerGPU(symmetric=False), geom, u,
+                                   ft.DeforModelRed3D, ft.DataCache(D))
+        compare(K, _oracle_form(O, femm, O.LIN_ELASTIC, geom, u, D, symmetric=False))
+        K32 = ft.bilform_lin_elastic(femm, ft.SysmatAssemblerGPU(symmetric=False,
+                                                                 precision="mixed"),
+                                     geom, u, ft.DeforModelRed3D, ft.DataCache(D))
+        x = rng.uniform(-1, 1, K.shape[0])
+        assert np.linalg.norm((K32 - K) @ x) / np.linalg.norm(K @ x) <= MIXED_TOL
+        untouched = np.setdiff1d(np.arange(1, n + 1), np.unique(conn))
+        rows = u.dofnums[untouched - 1].ravel() - 1
+        assert abs(K.tocsr()[rows]).sum() == 0 and abs(K32.tocsr()[rows]).sum() == 0
 
 
 @pytest.mark.parametrize("form", ["elastic", "convection"])
