@@ -70,25 +70,17 @@ __host__ __device__ constexpr int mixed_groups(int nne) {
   return n;
 }
 
-// FP64 Jacobian, determinant and inverse of one point (distorted elements).
-// det J and J^-1 (row-major) of a 3 x 3 Jacobian by cofactors, in FP64
+// det J and J^-1 (row-major, flat) of a 3 x 3 Jacobian by cofactors, in FP64
 __device__ __forceinline__ void inverse3_fp64(const double (&J)[3][3], double *inv, double &det) {
-  const double c0 = J[1][1] * J[2][2] - J[2][1] * J[1][2];
-  const double c1 = J[1][0] * J[2][2] - J[1][2] * J[2][0];
-  const double c2 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
-  det = J[0][0] * c0 - J[0][1] * c1 + J[0][2] * c2;
-  const double id = 1.0 / det;
-  inv[0] = c0 * id;
-  inv[1] = -(J[0][1] * J[2][2] - J[0][2] * J[2][1]) * id;
-  inv[2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
-  inv[3] = -c1 * id;
-  inv[4] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
-  inv[5] = -(J[0][0] * J[1][2] - J[1][0] * J[0][2]) * id;
-  inv[6] = (J[1][0] * J[2][1] - J[2][0] * J[1][1]) * id;
-  inv[7] = -(J[0][0] * J[2][1] - J[2][0] * J[0][1]) * id;
-  inv[8] = (J[0][0] * J[1][1] - J[1][0] * J[0][1]) * id;
+  double m[3][3];
+  det = det_inverse3<double, false, true>(J, m);
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) inv[r * 3 + c] = m[r][c];
 }
 
+// FP64 Jacobian, determinant and inverse of one point (distorted elements).
 template <int NNE, int MDIM>
 __device__ void jacobian_fp64(const double *xyz, const int32_t *conn, const double *dN, int sdim,
                               double *inv, double &det) {
