@@ -654,7 +654,7 @@ def test_mixed_precision(ft, O, et):
 
 
 @pytest.mark.parametrize("curved", [False, True])
-def test_mixed_t10_straight_and_curved(ft, curved):
+def test_mixed_t10_straight_and_curved(ft, O, curved):
     """Mixed T10 elasticity within the mixed bound of FP64 on straight-sided
     elements (affine: the FP32 corner Jacobian) and on elements whose
     mid-edge nodes are moved off the edges (curved: FP64 geometry), and on a
@@ -681,6 +681,12 @@ def test_mixed_t10_straight_and_curved(ft, curved):
     assert np.linalg.norm((K32 - K64) @ x) / np.linalg.norm(K64 @ x) <= MIXED_TOL
     assert abs(K32 - K64).max() / abs(K64).max() <= MIXED_TOL
     assert abs(K32 - K32.T).max() == 0.0
+    # the FP64 path against the oracle: corner Jacobians on the straight
+    # elements, isoparametric ones on the curved
+    D = ft.isotropic_D(70e9, 0.3)
+    K = ft.bilform_lin_elastic(femm, ft.SysmatAssemblerGPU(symmetric=False), geom, u,
+                               ft.DeforModelRed3D, ft.DataCache(D))
+    compare(K, _oracle_form(O, femm, O.LIN_ELASTIC, geom, u, D, symmetric=False))
 
 
 # ---------------------------------------------------------------- masslike
