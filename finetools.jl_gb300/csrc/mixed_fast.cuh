@@ -4,11 +4,15 @@
 // Same results as the tile of mixed.cuh (same FP32 arithmetic per block entry:
 // sums over the points in point order), organised for the FMA pipe:
 //   A. connectivity, FP32 coordinates relative to the element's first node
-//      (float4), Lame pair of the element;
+//      (float4), Lame pair of the element; T10: each mid-edge node tested
+//      against its edge midpoint (FP64);
 //   B. one thread per (element, point): J = X' dN, det J and J^-1 in FP32;
+//      a straight-sided T10 instead takes its constant corner Jacobian, J^-1
+//      and det J formed once in FP64 by the point-0 thread;
 //   B'. one thread per (element, point): distortion test over the element's
-//      points, FP64 J, det J, J^-1 for flagged elements, point weight w (det J
-//      times the rule weight, the other dimension and a scalar coefficient);
+//      points, FP64 J, det J, J^-1 for flagged elements (distorted, or curved
+//      T10), point weight w (det J times the rule weight, the other dimension
+//      and a scalar coefficient);
 //   C. one thread per (element, point, node): g = dN J^-1, stored with w as
 //      one float4 (g_x, g_y, g_z, w) at a padded slot (b + b/8, which keeps
 //      the four b's of a group in distinct shared-memory banks);
