@@ -165,12 +165,14 @@ def _oracle_t10_sample(n, reps):
     npts, Ns, dN, w, pc = femm.integrationdata()
     u = ft.numberdofs(ft.NodalField(np.zeros((fens.count(), 3))))
     D = ft.isotropic_D(210e9, 0.3)
-    times = []
+    times, phases = [], []
     for _ in range(reps):
         t = time.perf_counter()
-        O.bilform(O.LIN_ELASTIC, O.T10, fes.conn, fens.xyz, u.dofnums, u.nalldofs(), pc, w, D)
+        _, _, ph = O.bilform(O.LIN_ELASTIC, O.T10, fes.conn, fens.xyz, u.dofnums, u.nalldofs(),
+                             pc, w, D, phases=True)
         times.append(time.perf_counter() - t)
-    return fes.count(), times
+        phases.append(ph)
+    return fes.count(), times, phases
 
 
 _WORKER = {}
@@ -486,10 +488,17 @@ def run_ours(args):
 
     cpu = None
     if rank == 0 and not args.no_cpu:
-        ne, times = _oracle_t10_sample(CPU_SAMPLE_N, 3)
-        cpu = {"value": ne / min(times), "unit": "elements/s", "cores": 1, "kind": "port",
+        ne, times, phases = _oracle_t10_sample(CPU_SAMPLE_N, 3)
+        best = int(np.argmin(times))
+        ph = phases[best]
+        cpu = {"value": ne / times[best], "unit": "elements/s", "cores": 1, "kind": "port",
                "sample": f"T10 {CPU_SAMPLE_N}^3 block ({ne} elements), bilform_lin_elastic + "
-                         "makematrix! in the serial C restatement, best of 3"}
+                         "makematrix! in the serial C restatement, best of 3",
+               # the reference's phases: element loop with COO appends
+               # (assemble!), sparse() of the triples, S + S' completion
+               "phases_s": {"element_loop": float(ph[0]), "sparse": float(ph[1]),
+                            "symmetric_completion": float(ph[2])},
+               "host_cores": os.cpu_count()}
     if rank != 0:
         return
     out = {
