@@ -99,11 +99,10 @@ __device__ __forceinline__ void gather_node(const GArgs &g, int32_t A, float *ac
   const int cmax = g.maxdeg * NDN;
   const int cols = static_cast<int>(g.nptr[A + 1] - g.nptr[A]) * NDN;
   const GatherAcc<NDN> acc(accbase, cmax);
-  {
-    float4 *z = reinterpret_cast<float4 *>(accbase);
-    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int c = lane; c < (2 * NDN * cmax) / 4; c += 32) z[c] = zero;
-    for (int c = ((2 * NDN * cmax) / 4) * 4 + lane; c < 2 * NDN * cmax; c += 32) accbase[c] = 0.f;
+  // zero the node's own columns only (the others are not touched)
+  for (int c = lane; c < cols; c += 32) {
+    if constexpr (NDN == 3) acc.a01[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+    acc.a2[c] = make_float2(0.f, 0.f);
   }
   // the lane's (b, j) tasks, fixed for all incident elements
   int tb[NSLOT], tj[NSLOT], trow[NSLOT];
