@@ -15,7 +15,7 @@ LIBPATH = os.path.join(HERE, "libfegpu.so")
 OK = 0
 Q4, H8, H20, T4, T10 = 0, 1, 2, 3, 4
 COEF_CONST, COEF_PER_ELEMENT, COEF_PER_QP, COEF_ISO_LAME = 0, 1, 2, 3
-FP64, MIXED = 0, 1
+FP64, MIXED, FP64_FAST = 0, 1, 2
 FORM_DIFFUSION, FORM_LIN_ELASTIC, FORM_DOT = 0, 1, 2
 REQUEST_COEF, REQUEST_COORDS = 0, 1
 ASM_SPARSE, ASM_SPARSE_SYMM, ASM_SPARSE_DIAG, ASM_HRZ_LUMPING_SYMM = 0, 1, 2, 3
@@ -26,7 +26,7 @@ EXPORTS = [
     "fegpu_context_kernel_stats", "fegpu_femm_create", "fegpu_femm_destroy",
     "fegpu_femm_set_geometry", "fegpu_femm_set_axisymmetric", "fegpu_femm_colors", "fegpu_dofmap_create",
     "fegpu_dofmap_destroy", "fegpu_dofmap_copy_pattern", "fegpu_matrix_create",
-    "fegpu_matrix_destroy", "fegpu_bilform_diffusion", "fegpu_bilform_lin_elastic",
+    "fegpu_matrix_destroy", "fegpu_matrix_set_symmetric_assembly", "fegpu_bilform_diffusion", "fegpu_bilform_lin_elastic",
     "fegpu_bilform_dot", "fegpu_bilform_div_grad", "fegpu_bilform_convection", "fegpu_linform_dot", "fegpu_bilform_dot_lumped", "fegpu_matrix_nnz", "fegpu_matrix_copy_csc",
     "fegpu_matrix_copy_values", "fegpu_matrix_copy_values_async", "fegpu_matrix_wait_export", "fegpu_matrix_copy_block_csc", "fegpu_matrix_spmv",
     "fegpu_matrix_cg", "fegpu_assembler_create",
@@ -82,6 +82,7 @@ def load(path: str = LIBPATH):
         "fegpu_dofmap_copy_pattern": ([vp, vp, vp], i32),
         "fegpu_matrix_create": ([vp, pp], i32),
         "fegpu_matrix_destroy": ([vp], i32),
+        "fegpu_matrix_set_symmetric_assembly": ([vp, i32], i32),
         "fegpu_bilform_diffusion": ([vp, C.POINTER(Coef), i32], i32),
         "fegpu_bilform_lin_elastic": ([vp, C.POINTER(Coef), i32], i32),
         "fegpu_bilform_div_grad": ([vp, C.POINTER(Coef), i32], i32),

@@ -104,7 +104,10 @@ class SysmatAssemblerGPU:
 
     symmetric=True reproduces SysmatAssemblerSparseSymm (the default of the
     symmetric forms: exact zeros of S + S' are not stored), symmetric=False
-    SysmatAssemblerSparse (structural pattern kept).  precision "fp64" or
+    SysmatAssemblerSparse (structural pattern kept).  precision "fp64" (the
+    reference's operation order: bilform_diffusion and bilform_lin_elastic
+    return the reference algorithm's matrix bit for bit), "fp64_fast" (FP64
+    with fused multiply-adds: within 1e-12 |K_ij| + 1e-14 max_k |K_ik|) or
     "mixed" (FP32 element arithmetic, FP64 global accumulation).  lumping
     "diag" / "hrz" reproduces SysmatAssemblerSparseDiag /
     SysmatAssemblerSparseHRZLumpingSymm (diagonal results; bilform_dot and the
@@ -113,8 +116,8 @@ class SysmatAssemblerGPU:
 
     def __init__(self, symmetric: bool = True, precision: str = "fp64", result: str = "host",
                  drop_zeros=None, device: int = 0, lumping=None):
-        if precision not in ("fp64", "mixed"):
-            raise ValueError("precision must be 'fp64' or 'mixed'")
+        if precision not in ("fp64", "fp64_fast", "mixed"):
+            raise ValueError("precision must be 'fp64', 'fp64_fast' or 'mixed'")
         if lumping not in (None, "diag", "hrz"):
             raise ValueError("lumping must be None, 'diag' or 'hrz'")
         self.lumping = lumping
@@ -122,7 +125,8 @@ class SysmatAssemblerGPU:
             raise ValueError("result must be 'host' or 'device'")
         self.symmetric = symmetric
         self.precision = precision
-        self.precision_code = nat.FP64 if precision == "fp64" else nat.MIXED
+        self.precision_code = {"fp64": nat.FP64, "fp64_fast": nat.FP64_FAST,
+                               "mixed": nat.MIXED}[precision]
         self.result = result
         self.drop_zeros = symmetric if drop_zeros is None else bool(drop_zeros)
         self.device = device
@@ -153,6 +157,7 @@ class SysmatAssemblerGPU:
             nat.check(nat.load().fegpu_matrix_create(dm.h, C.byref(out)))
             h = out.value
             dm.matrices[key] = h
+        nat.check(nat.load().fegpu_matrix_set_symmetric_assembly(h, int(bool(self.symmetric))))
         return h
 
     def _run(self, dm, call):

@@ -87,7 +87,7 @@ int choose_tile(int etype, int form, int precision, int npts) {
   te = std::max(1, std::min(te, want));
   // FEGPU_FP64_TILE overrides the elements per tile of the FP64 colour
   // kernels (tuning; capped by the shared memory of one CTA)
-  if (precision == FEGPU_FP64) {
+  if (precision != FEGPU_MIXED) {
     if (const char *env = std::getenv("FEGPU_FP64_TILE")) {
       const int v = std::atoi(env);
       if (v > 0) {
@@ -421,9 +421,21 @@ bool is_isotropic(const double *D, double &lam, double &mu) {
   return true;
 }
 
-namespace {
+bool iso_pattern(const double *D, double &d0, double &d1, double &d3) {
+  d0 = D[0];
+  d1 = D[1];
+  d3 = D[3 * 6 + 3];
+  for (int i = 0; i < 6; ++i)
+    for (int j = 0; j < 6; ++j) {
+      double expect;
+      if (i < 3 && j < 3) expect = (i == j) ? d0 : d1;
+      else if (i == j) expect = d3;
+      else expect = 0.0;
+      if (D[i * 6 + j] != expect) return false;
+    }
+  return true;
+}
 
-}  // namespace
 }  // namespace fegpu
 
 using namespace fegpu;
@@ -717,6 +729,13 @@ int fegpu_matrix_destroy(fegpu_matrix *K) {
   });
 }
 
+int fegpu_matrix_set_symmetric_assembly(fegpu_matrix *K, int symmetric) {
+  return guarded([&] {
+    FEGPU_REQUIRE(K, "null handle");
+    K->symm_asm = symmetric != 0;
+  });
+}
+
 static void zero_matrix(fegpu_matrix *K) {
   FEGPU_CUDA(cudaMemsetAsync(K->val.p, 0, sizeof(double) * K->dm->nnz, K->dm->femm->ctx->stream));
 }
@@ -730,7 +749,9 @@ int fegpu_bilform_diffusion(fegpu_matrix *K, const fegpu_coef *cf, int precision
     require_geometry(fm);
     FEGPU_REQUIRE(dm->ndn == 1, "diffusion: the field must have one DOF per node");
     FEGPU_REQUIRE(fm->sdim == fm->mdim, "diffusion: the element must fill the space");
-    FEGPU_REQUIRE(precision == FEGPU_FP64 || precision == FEGPU_MIXED, "unknown precision");
+    FEGPU_REQUIRE(precision == FEGPU_FP64 || precision == FEGPU_MIXED ||
+                      precision == FEGPU_FP64_FAST,
+                  "unknown precision");
     const int md = fm->mdim;
     int form;
     if (cf->ncomp == 1) {
@@ -745,10 +766,16 @@ int fegpu_bilform_diffusion(fegpu_matrix *K, const fegpu_coef *cf, int precision
     K->unsym = false;
     KArgs a = base_args(K, dm);
     CoefStage st;
-    const bool gather = precision == FEGPU_MIXED;
+    const bool exact = precision == FEGPU_FP64;
+    const bool gather = precision == FEGPU_MIXED || exact;
     stage_coef(fm, cf, cf->ncomp, a, st, !gather);
-    if (!gather) zero_matrix(K);
-    if (fm->nelem > 0) run_form(dm, form, precision, a);
+    if (exact) {
+      if (fm->nelem > 0) run_exact(dm, form, a, K->symm_asm);
+      else zero_matrix(K);
+    } else {
+      if (!gather) zero_matrix(K);
+      if (fm->nelem > 0) run_form(dm, form, precision, a);
+    }
     FEGPU_CUDA(cudaStreamSynchronize(fm->ctx->stream));  // st owns the staged data
   });
 }
@@ -762,11 +789,46 @@ int fegpu_bilform_lin_elastic(fegpu_matrix *K, const fegpu_coef *cf, int precisi
     require_geometry(fm);
     FEGPU_REQUIRE(fm->mdim == 3 && fm->sdim == 3, "lin_elastic: 3-D solid elements only");
     FEGPU_REQUIRE(dm->ndn == 3, "lin_elastic: the field must have three DOFs per node");
-    FEGPU_REQUIRE(precision == FEGPU_FP64 || precision == FEGPU_MIXED, "unknown precision");
+    FEGPU_REQUIRE(precision == FEGPU_FP64 || precision == FEGPU_MIXED ||
+                      precision == FEGPU_FP64_FAST,
+                  "unknown precision");
     K->unsym = false;
     KArgs a = base_args(K, dm);
     CoefStage st;
     int form;
+    if (precision == FEGPU_FP64) {
+      // reference order: the 6x6 D entries themselves (an isotropic pattern
+      // skips D's zeros), per-element (lambda, mu) pairs formed into D's
+      // entries on the device as the 6x6 D is formed
+      if (cf->kind == FEGPU_COEF_ISO_LAME) {
+        form = F_ELAST_ISO;
+        stage_coef(fm, cf, 2, a, st, false);
+      } else if (cf->kind == FEGPU_COEF_CONST && cf->ncomp == 36) {
+        double d0, d1, d3;
+        if (iso_pattern(cf->data, d0, d1, d3)) {
+          form = F_ELAST_ISO;
+          a.coef_kind = FEGPU_COEF_CONST;
+          a.ncomp = 3;
+          a.cconst[0] = d0;
+          a.cconst[1] = d1;
+          a.cconst[2] = d3;
+        } else {
+          form = F_ELAST_GEN;
+          stage_coef(fm, cf, 36, a, st, false);
+        }
+      } else if (cf->kind == FEGPU_COEF_PER_ELEMENT && cf->ncomp == 36) {
+        form = F_ELAST_GEN;
+        stage_coef(fm, cf, 36, a, st, false);
+      } else {
+        throw Error{FEGPU_ERR_ARG,
+                    "lin_elastic: coefficient must be a 6x6 D (constant or per element) or "
+                    "per-element (lambda, mu)"};
+      }
+      if (fm->nelem > 0) run_exact(dm, form, a, K->symm_asm);
+      else zero_matrix(K);
+      FEGPU_CUDA(cudaStreamSynchronize(fm->ctx->stream));
+      return;
+    }
     const bool gather = precision == FEGPU_MIXED;
     if (cf->kind == FEGPU_COEF_ISO_LAME) {
       form = F_ELAST_ISO;
@@ -810,7 +872,12 @@ int fegpu_bilform_div_grad(fegpu_matrix *K, const fegpu_coef *cf, int precision)
     require_geometry(fm);
     FEGPU_REQUIRE(fm->mdim == 3 && fm->sdim == 3 && dm->ndn == 3,
                   "div_grad: 3-D elements with a three-component field");
-    FEGPU_REQUIRE(precision == FEGPU_FP64 || precision == FEGPU_MIXED, "unknown precision");
+    FEGPU_REQUIRE(precision == FEGPU_FP64 || precision == FEGPU_MIXED ||
+                      precision == FEGPU_FP64_FAST,
+                  "unknown precision");
+    // FP64: the colour kernels of the elasticity form (lambda = 0), whose
+    // element blocks are the div_grad blocks in another association
+    if (precision == FEGPU_FP64) precision = FEGPU_FP64_FAST;
     FEGPU_REQUIRE(cf->ncomp == 1, "div_grad: the viscosity must be a scalar");
     K->unsym = false;
     KArgs a = base_args(K, dm);

@@ -1,0 +1,272 @@
+// Reference-order FP64 assembly: plan, row gather and orchestration (the
+// element blocks are k_blocks_exact of exact.cuh, instantiated per element
+// type in forms_<type>.cu).
+//
+// The gather sums each CSR entry over the incident elements in element order
+// with separately rounded FP64 adds, in two buckets that are the reference's
+// S(r, c) and S(c, r) (SysmatAssemblerSparseSymm's assemble! keeps the lower
+// triangle by local index; sparse() sums duplicates in input order;
+// makematrix! returns S + S' with the diagonal halved,
+// src/AssemblyModule.jl:500-583).  An empty bucket starts as -0.0, which the
+// first addition replaces exactly, so every stored value is the reference's
+// value bit for bit; exact zeros are left out at export (drop_zeros) as the
+// reference's sparse `+` leaves them out.
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#include "exact.cuh"
+#include "forms_dispatch.cuh"
+
+namespace fegpu {
+namespace {
+
+constexpr int kExactGatherWarps = 8;
+
+// doubles of shared memory per warp: the node's NDN rows, one or two buckets
+__host__ __device__ inline int exact_warp_stride(int ndn, int maxdeg, bool sym) {
+  return (sym ? 2 : 1) * ndn * maxdeg * ndn;
+}
+
+template <int NNE, int NDN, bool SYM>
+__device__ __forceinline__ void gather_node_exact(const GArgs &g, int32_t A, double *acc,
+                                                  int lane) {
+  constexpr int NBLK = NNE * (NNE + 1) / 2;
+  constexpr int BS = NDN * NDN;
+  constexpr int NTASK = NNE * NDN;  // (b, j): node of the element, column component
+  constexpr int NSLOT = (NTASK + 31) / 32;
+  const int cmax = g.maxdeg * NDN;
+  const int cols = static_cast<int>(g.nptr[A + 1] - g.nptr[A]) * NDN;
+  double *lo = acc;                // S(r, c): local row index >= local column index
+  double *up = acc + NDN * cmax;   // S(c, r) (symmetric assembly only)
+  for (int c = lane; c < cols; c += 32)
+#pragma unroll
+    for (int i = 0; i < NDN; ++i) {
+      lo[i * cmax + c] = -0.0;
+      if (SYM) up[i * cmax + c] = -0.0;
+    }
+  int tb[NSLOT], tj[NSLOT], trow[NSLOT];
+#pragma unroll
+  for (int s = 0; s < NSLOT; ++s) {
+    const int task = min(lane + 32 * s, NTASK - 1);
+    tb[s] = task / NDN;
+    tj[s] = task - tb[s] * NDN;
+    trow[s] = tb[s] * NNE - tb[s] * (tb[s] - 1) / 2 - tb[s];  // pair(b, x) = trow + x, x >= b
+  }
+  __syncwarp();
+  const int64_t qa = g.n2e_ptr[A], qz = g.n2e_ptr[A + 1];
+  int self = 0;  // position of A in its own neighbour list (its diagonal)
+  for (int64_t q = qa; q < qz; ++q) {
+    const int32_t e = g.n2e_elem[q];
+    const int a = g.n2e_loc[q];
+    const int32_t ch = static_cast<int32_t>(g.chunk);
+    const int32_t ce = e / ch;
+    const int64_t slot = static_cast<int64_t>(ce % g.ring) * ch + (e - ce * ch);
+    const double *kb = g.ke64 + slot * NBLK * BS;
+    const uint16_t *pe = g.pos + (static_cast<int64_t>(e) * NNE + a) * NNE;
+    if (q == qa) self = pe[a];
+    const int rowa = a * NNE - a * (a - 1) / 2 - a;
+#pragma unroll
+    for (int s = 0; s < NSLOT; ++s) {
+      if (lane + 32 * s >= NTASK) break;
+      const int b = tb[s], j = tj[s];
+      const bool upper = a <= b;  // block (a, b) stored; else (b, a), transposed
+      const double *blk = kb + (upper ? rowa + b : trow[s] + a) * BS + (upper ? j : j * NDN);
+      const int step = upper ? NDN : 1;
+      const int col = pe[b] * NDN + j;
+#pragma unroll
+      for (int i = 0; i < NDN; ++i) {
+        const double v = blk[i * step];
+        double *dst = lo;
+        if (SYM && a * NDN + i < b * NDN + j) dst = up;
+        dst += i * cmax + col;
+        *dst = __dadd_rn(*dst, v);
+      }
+    }
+    __syncwarp();
+  }
+  int64_t base[NDN];
+#pragma unroll
+  for (int i = 0; i < NDN; ++i) base[i] = g.rowptr[g.dof[A * NDN + i]];
+  for (int c = lane; c < cols; c += 32) {
+    const int64_t off = g.colperm ? g.colperm[g.cpoff[A] * NDN + c] : c;
+#pragma unroll
+    for (int i = 0; i < NDN; ++i) {
+      const double l = lo[i * cmax + c];
+      double v = l;
+      if (SYM) {
+        // S + S': (S + S) / 2 on the diagonal
+        v = (c == self * NDN + i) ? __dmul_rn(__dadd_rn(l, l), 0.5) : __dadd_rn(l, up[i * cmax + c]);
+      }
+      g.val[base[i] + off] = v;
+    }
+  }
+  __syncwarp();
+}
+
+template <int NNE, int NDN, bool SYM>
+__global__ void __launch_bounds__(kExactGatherWarps * 32) k_gather_exact(const GArgs g) {
+  extern __shared__ __align__(16) double xsm[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double *acc = xsm + static_cast<size_t>(warp) * exact_warp_stride(NDN, g.maxdeg, SYM);
+  for (int64_t t = g.n0 + static_cast<int64_t>(blockIdx.x) * kExactGatherWarps + warp; t < g.n1;
+       t += static_cast<int64_t>(gridDim.x) * kExactGatherWarps)
+    gather_node_exact<NNE, NDN, SYM>(g, g.nodes[t], acc, lane);
+}
+
+template <int NNE, int NDN, bool SYM>
+int launch_gx(const GArgs &g, int num_sms, cudaStream_t s) {
+  const int64_t n = g.n1 - g.n0;
+  if (n <= 0) return 0;
+  const size_t smem =
+      sizeof(double) * static_cast<size_t>(exact_warp_stride(NDN, g.maxdeg, SYM)) * kExactGatherWarps;
+  FEGPU_REQUIRE(smem <= 227 * 1024, "node degree too large for the row gather");
+  auto kern = k_gather_exact<NNE, NDN, SYM>;
+  FEGPU_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  static_cast<int>(smem)));
+  int per_sm = 0;
+  FEGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kExactGatherWarps * 32,
+                                                           smem));
+  per_sm = std::max(per_sm, 1);
+  const int64_t ctas = (n + kExactGatherWarps - 1) / kExactGatherWarps;
+  const int grid = static_cast<int>(std::min<int64_t>(ctas, static_cast<int64_t>(num_sms) * per_sm));
+  kern<<<grid, kExactGatherWarps * 32, smem, s>>>(g);
+  FEGPU_CUDA(cudaGetLastError());
+  return 1;
+}
+
+template <int NNE>
+int launch_gx_nne(int ndn, bool sym, const GArgs &g, int num_sms, cudaStream_t s) {
+  if (ndn == 1) return sym ? launch_gx<NNE, 1, true>(g, num_sms, s) : launch_gx<NNE, 1, false>(g, num_sms, s);
+  return sym ? launch_gx<NNE, 3, true>(g, num_sms, s) : launch_gx<NNE, 3, false>(g, num_sms, s);
+}
+
+int launch_gather_exact(int etype, int ndn, bool sym, const GArgs &g, int num_sms, cudaStream_t s) {
+  switch (etype) {
+    case FEGPU_Q4: return launch_gx_nne<4>(ndn, sym, g, num_sms, s);
+    case FEGPU_H8: return launch_gx_nne<8>(ndn, sym, g, num_sms, s);
+    case FEGPU_H20: return launch_gx_nne<20>(ndn, sym, g, num_sms, s);
+    case FEGPU_T4: return launch_gx_nne<4>(ndn, sym, g, num_sms, s);
+    case FEGPU_T10: return launch_gx_nne<10>(ndn, sym, g, num_sms, s);
+  }
+  throw Error{FEGPU_ERR_ARG, "unknown element type"};
+}
+
+int launch_exact(int etype, int form, const KArgs &a, int num_sms, cudaStream_t s) {
+  switch (etype) {
+    case FEGPU_Q4: return launch_exact_q4(form, a, num_sms, s);
+    case FEGPU_H8: return launch_exact_h8(form, a, num_sms, s);
+    case FEGPU_H20: return launch_exact_h20(form, a, num_sms, s);
+    case FEGPU_T4: return launch_exact_t4(form, a, num_sms, s);
+    case FEGPU_T10: return launch_exact_t10(form, a, num_sms, s);
+  }
+  throw Error{FEGPU_ERR_ARG, "unknown element type"};
+}
+
+// chunks of ~16 MB of FP64 blocks (at least 256 elements); the ring of span +
+// 2 chunks then stays near the size of the L2
+void build_exact_plan(fegpu_dofmap *dm, int block_values) {
+  fegpu_femm *fm = dm->femm;
+  cudaStream_t s = fm->ctx->stream;
+  const int64_t E = fm->nelem;
+  build_node_lists(dm, nullptr);
+  const int64_t per_elem = static_cast<int64_t>(block_values) * 8;
+  dm->x_chunk = std::max<int64_t>(256, (16ll << 20) / std::max<int64_t>(per_elem, 1));
+  dm->x_chunk = std::min<int64_t>(dm->x_chunk, std::max<int64_t>(E, 1));
+  std::vector<int32_t> order;
+  plan_chunks(dm, dm->x_chunk, dm->x_chunk_nodes, order, dm->x_span, dm->x_ring);
+  dm->x_gnodes.alloc(sizeof(int32_t) * std::max<size_t>(order.size(), 1));
+  if (!order.empty())
+    FEGPU_CUDA(cudaMemcpyAsync(dm->x_gnodes.p, order.data(), sizeof(int32_t) * order.size(),
+                               cudaMemcpyHostToDevice, s));
+  dm->x_ke.alloc(sizeof(double) * static_cast<size_t>(dm->x_ring) * dm->x_chunk * block_values);
+  FEGPU_CUDA(cudaStreamSynchronize(s));
+  dm->exact_ready = true;
+}
+
+}  // namespace
+
+// elements per tile of the reference-order block kernel: the shared memory
+// of two CTAs per SM (one for the largest elements), at least one element
+int exact_tile(int etype, int form, int npts) {
+  const int nne = nodes_per_elem(etype), mdim = manif_dim(etype);
+  const size_t one = exact_layout(nne, mdim, npts, 1, form).total;
+  const size_t two = exact_layout(nne, mdim, npts, 2, form).total;
+  const size_t per = two - one;
+  const size_t fixed = one - per;
+  const size_t budget = per > 24 * 1024 ? 220 * 1024 : 110 * 1024;
+  int te = static_cast<int>((budget - std::min(budget, fixed)) / std::max<size_t>(per, 1));
+  te = std::max(1, std::min(te, 64));
+  FEGPU_REQUIRE(exact_layout(nne, mdim, npts, te, form).total <= 227 * 1024,
+                "quadrature rule too large for the reference-order element kernel");
+  return te;
+}
+
+// Element blocks of chunk c on the side stream, the gather of the nodes that
+// chunk completes on the context stream (as the mixed path runs).
+void run_exact(fegpu_dofmap *dm, int form, KArgs &a, bool symmetric) {
+  fegpu_femm *fm = dm->femm;
+  fegpu_context *ctx = fm->ctx;
+  const int nne = fm->nne, ndn = dm->ndn;
+  const int bs = ndn * ndn, nblk = nne * (nne + 1) / 2;
+  if (!dm->exact_ready) build_exact_plan(dm, nblk * bs);
+  a.conn = fm->conn_orig.as<int32_t>();
+  a.te = exact_tile(fm->etype, form, fm->npts);
+  GArgs g;
+  std::memset(&g, 0, sizeof(g));
+  g.n2e_ptr = dm->n2e_ptr.as<int64_t>();
+  g.n2e_elem = dm->n2e_elem.as<int32_t>();
+  g.n2e_loc = dm->n2e_loc.as<uint8_t>();
+  g.nodes = dm->x_gnodes.as<int32_t>();
+  g.nptr = dm->nptr.as<int64_t>();
+  g.pos = dm->pos_orig.as<uint16_t>();
+  g.ke64 = dm->x_ke.as<double>();
+  g.chunk = dm->x_chunk;
+  g.ring = dm->x_ring;
+  g.dof = dm->dof.as<int32_t>();
+  g.rowptr = dm->rowptr.as<int64_t>();
+  g.colperm = dm->contiguous ? nullptr : dm->colperm.as<int32_t>();
+  g.cpoff = dm->contiguous ? nullptr : dm->cpoff.as<int64_t>();
+  g.val = a.val;
+  g.maxdeg = dm->maxdeg;
+  const int64_t nch = static_cast<int64_t>(dm->x_chunk_nodes.size()) - 1;
+  cudaStream_t s0 = ctx->stream;
+  if (!ctx->side) FEGPU_CUDA(cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking));
+  while (static_cast<int>(ctx->ev_blocks.size()) < dm->x_ring) {
+    cudaEvent_t e1, e2;
+    FEGPU_CUDA(cudaEventCreateWithFlags(&e1, cudaEventDisableTiming));
+    FEGPU_CUDA(cudaEventCreateWithFlags(&e2, cudaEventDisableTiming));
+    ctx->ev_blocks.push_back(e1);
+    ctx->ev_gather.push_back(e2);
+  }
+  if (ctx->timing) FEGPU_CUDA(cudaEventRecord(ctx->ev0, s0));
+  FEGPU_CUDA(cudaEventRecord(ctx->ev_gather[0], s0));  // work before this call
+  FEGPU_CUDA(cudaStreamWaitEvent(ctx->side, ctx->ev_gather[0], 0));
+  for (int64_t c = 0; c < nch; ++c) {
+    const int slot = static_cast<int>(c % dm->x_ring);
+    if (c >= dm->x_ring) {
+      const int64_t reader = c - dm->x_ring + dm->x_span;  // last gather reading the slot
+      FEGPU_CUDA(cudaStreamWaitEvent(ctx->side, ctx->ev_gather[reader % dm->x_ring], 0));
+    }
+    a.e0 = c * dm->x_chunk;
+    a.e1 = std::min(fm->nelem, (c + 1) * dm->x_chunk);
+    a.ke64 = dm->x_ke.as<double>() + slot * dm->x_chunk * nblk * bs;
+    ctx->launches += launch_exact(fm->etype, form, a, ctx->num_sms, ctx->side);
+    FEGPU_CUDA(cudaEventRecord(ctx->ev_blocks[slot], ctx->side));
+    FEGPU_CUDA(cudaStreamWaitEvent(s0, ctx->ev_blocks[slot], 0));
+    g.n0 = dm->x_chunk_nodes[c];
+    g.n1 = dm->x_chunk_nodes[c + 1];
+    ctx->launches += launch_gather_exact(fm->etype, ndn, symmetric, g, ctx->num_sms, s0);
+    FEGPU_CUDA(cudaEventRecord(ctx->ev_gather[slot], s0));
+  }
+  if (ctx->timing) {
+    FEGPU_CUDA(cudaEventRecord(ctx->ev1, s0));
+    FEGPU_CUDA(cudaEventSynchronize(ctx->ev1));
+    float ms = 0.f;
+    FEGPU_CUDA(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+    ctx->kernel_ms += ms;
+  }
+}
+
+}  // namespace fegpu

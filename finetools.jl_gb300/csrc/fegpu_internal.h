@@ -136,6 +136,8 @@ struct fegpu_dofmap {
   fegpu::DevBuf colperm;    // int32 per node block, only if !contiguous
   fegpu::DevBuf cpoff;      // int64 [nnodes], only if !contiguous
   fegpu::DevBuf nptr;       // int64 [nnodes + 1]: node adjacency offsets
+  // node -> element lists in element order (gather.cu), built on first use
+  bool lists_ready = false;
   // row-gather plan (mixed precision), built on first use
   bool gather_ready = false;
   int64_t chunk = 0;        // elements per chunk of the block ring
@@ -150,6 +152,14 @@ struct fegpu_dofmap {
   fegpu::DevBuf pos_orig;   // uint16 [nelem][nne][nne], element order
   fegpu::DevBuf ke;         // float ring of element blocks
   std::vector<int32_t> node_first, node_last;  // first / last incident element (-1: none)
+  // reference-order FP64 path (exact.cu): its own chunk plan over the same
+  // node-to-element lists, and an FP64 block ring
+  bool exact_ready = false;
+  int64_t x_chunk = 0;
+  int x_ring = 0, x_span = 0;
+  std::vector<int64_t> x_chunk_nodes;
+  fegpu::DevBuf x_gnodes;   // int32: nodes in gather order
+  fegpu::DevBuf x_ke;       // double ring of element blocks
   // plan of the allocation-free variant (noalloc.cu), cached per chunk size
   int64_t na_chunk = 0;
   int na_ring = 0;
@@ -162,6 +172,7 @@ struct fegpu_matrix {
   fegpu_dofmap *dm = nullptr;
   fegpu::DevBuf val;    // double [nnz], CSR order (row = test DOF)
   bool unsym = false;   // values not symmetric: the CSC export transposes them
+  bool symm_asm = true; // SysmatAssemblerSparseSymm (S + S') or SysmatAssemblerSparse (S)
   // asynchronous export: `ready` marks the values on the context stream,
   // `exported` the end of their copy on the export stream
   cudaEvent_t ready = nullptr, exported = nullptr;
@@ -207,6 +218,7 @@ struct KArgs {
   int64_t e0, e1;          // colour range of sorted elements
   int *status;             // device status word (0 = ok)
   float *ke;               // block-output mode: element blocks of elements e0.. (or null)
+  double *ke64;            // reference-order path: FP64 blocks of elements e0..
 };
 
 // Launch one colour of one form.  Returns the number of kernel launches made.
@@ -233,6 +245,7 @@ struct GArgs {
   const int64_t *nptr;      // adjacency offsets (degree)
   const uint16_t *pos;      // element-order slot maps
   const float *ke;          // ring of element blocks
+  const double *ke64;       // ring of FP64 element blocks (reference-order path)
   int64_t chunk;            // elements per ring chunk
   int ring;                 // chunks in the ring
   const int32_t *dof;
@@ -243,11 +256,24 @@ struct GArgs {
   int maxdeg;
 };
 void build_gather_plan(fegpu_dofmap *dm, int nblk_values);
+// node -> element lists and element-order slot maps (once per dofmap); the
+// host copy of the lists goes to elem_out when given
+void build_node_lists(fegpu_dofmap *dm, std::vector<int32_t> *elem_out);
+// gather order and ring size for chunks of `chunk` elements
+void plan_chunks(const fegpu_dofmap *dm, int64_t chunk, std::vector<int64_t> &chunk_nodes,
+                 std::vector<int32_t> &order, int &span, int &ring);
 int launch_gather(int etype, int ndn, const GArgs &g, int num_sms, cudaStream_t s);
 // variant that computes each element's ring slot from chunk and ring
 // (g.n2e_slot unused)
 int launch_gather_inline_slot(int etype, int ndn, const GArgs &g, int num_sms, cudaStream_t s);
 int launch_mixed(int etype, int form, const KArgs &a, int sms, cudaStream_t s);
+// reference-order FP64 path (exact.cu): elements per tile of its block kernel,
+// and the whole assembly (blocks + element-order two-bucket gather) into a.val
+int exact_tile(int etype, int form, int npts);
+void run_exact(fegpu_dofmap *dm, int form, KArgs &a, bool symmetric);
+// D has the isotropic zero pattern with equal normal diagonal (d0), normal
+// off-diagonal (d1) and shear diagonal (d3) entries
+bool iso_pattern(const double *D, double &d0, double &d1, double &d3);
 // elements per tile and the tile's shared memory for a form of the mixed path
 // elements per mixed tile: wide = the persistent batch kernel's tile shape
 int mixed_tile_for(int etype, int form, int npts, bool wide = true);

@@ -6,6 +6,7 @@
 #include <cstdlib>
 
 #include "elements.cuh"
+#include "exact.cuh"
 #include "mixed_fast.cuh"
 #include "mixed_tc.cuh"
 
@@ -59,6 +60,28 @@ int launch_mixed_et(int form, const KArgs &a, int sms, cudaStream_t s) {
   throw Error{FEGPU_ERR_ARG, "mixed precision: form not available for this element type"};
 }
 
+// Reference-order FP64 element blocks (exact.cuh) for the row gather of exact.cu.
+template <int ET>
+int launch_exact_et(int form, const KArgs &a, int sms, cudaStream_t s) {
+  constexpr bool SOLID = ElemT<ET>::MDIM == 3;
+  switch (form) {
+    case F_DIFF_ISO: return launch_blocks_exact_t<ET, F_DIFF_ISO>(a, sms, s);
+    case F_DIFF_GEN: return launch_blocks_exact_t<ET, F_DIFF_GEN>(a, sms, s);
+    case F_ELAST_ISO:
+      if constexpr (SOLID) return launch_blocks_exact_t<ET, F_ELAST_ISO>(a, sms, s);
+      break;
+    case F_ELAST_GEN:
+      if constexpr (SOLID) return launch_blocks_exact_t<ET, F_ELAST_GEN>(a, sms, s);
+      break;
+  }
+  throw Error{FEGPU_ERR_ARG, "reference-order FP64: form not available for this element type"};
+}
+
+int launch_exact_q4(int, const KArgs &, int, cudaStream_t);
+int launch_exact_h8(int, const KArgs &, int, cudaStream_t);
+int launch_exact_h20(int, const KArgs &, int, cudaStream_t);
+int launch_exact_t4(int, const KArgs &, int, cudaStream_t);
+int launch_exact_t10(int, const KArgs &, int, cudaStream_t);
 int launch_form_q4(int, int, int, const KArgs &, int, cudaStream_t);
 int launch_form_h8(int, int, int, const KArgs &, int, cudaStream_t);
 int launch_form_h20(int, int, int, const KArgs &, int, cudaStream_t);

@@ -88,20 +88,17 @@ int launch_gather_inline_slot(int etype, int ndn, const GArgs &g, int num_sms, c
   throw Error{FEGPU_ERR_ARG, "unknown element type"};
 }
 
-// Node -> element lists, chunk plan and element-order slot maps.
-void build_gather_plan(fegpu_dofmap *dm, int block_values) {
+// Node -> element lists (incident elements in element order, with the node's
+// local index) and the element-order slot maps: built once per dofmap, shared
+// by the mixed and the reference-order chunk plans.  elem_out (optional)
+// receives the host copy of the element lists.
+void build_node_lists(fegpu_dofmap *dm, std::vector<int32_t> *elem_out) {
   fegpu_femm *fm = dm->femm;
   fegpu_context *ctx = fm->ctx;
   cudaStream_t s = ctx->stream;
   const int nne = fm->nne;
   const int64_t N = fm->nnodes, E = fm->nelem;
   const std::vector<int32_t> &c0 = fm->conn_host;
-  // chunk: ~24 MB of FP32 blocks, at least 1024 elements
-  const int64_t per_elem = static_cast<int64_t>(block_values) * 4;
-  dm->chunk = std::max<int64_t>(1024, (24ll << 20) / std::max<int64_t>(per_elem, 1));
-  dm->chunk = std::min<int64_t>(dm->chunk, std::max<int64_t>(E, 1));
-  const int64_t nch = (E + dm->chunk - 1) / dm->chunk;
-  // node -> elements (increasing) with local indices
   std::vector<int64_t> ptr(N + 1, 0);
   for (int64_t i = 0; i < E * nne; ++i) ptr[c0[i] + 1]++;
   for (int64_t n = 0; n < N; ++n) ptr[n + 1] += ptr[n];
@@ -114,8 +111,6 @@ void build_gather_plan(fegpu_dofmap *dm, int block_values) {
       elem[q] = static_cast<int32_t>(e);
       loc[q] = static_cast<uint8_t>(a);
     }
-  std::vector<int32_t> slot(elem.size());
-  // a node is gathered after the chunk of its last element
   dm->node_first.assign(N, -1);
   dm->node_last.assign(N, -1);
   for (int64_t n = 0; n < N; ++n)
@@ -123,28 +118,79 @@ void build_gather_plan(fegpu_dofmap *dm, int block_values) {
       dm->node_first[n] = elem[ptr[n]];
       dm->node_last[n] = elem[ptr[n + 1] - 1];
     }
+  if (!dm->lists_ready) {
+    dm->n2e_ptr.alloc(sizeof(int64_t) * (N + 1));
+    dm->n2e_elem.alloc(sizeof(int32_t) * std::max<size_t>(elem.size(), 1));
+    dm->n2e_loc.alloc(std::max<size_t>(loc.size(), 1));
+    FEGPU_CUDA(cudaMemcpyAsync(dm->n2e_ptr.p, ptr.data(), sizeof(int64_t) * (N + 1),
+                               cudaMemcpyHostToDevice, s));
+    if (!elem.empty()) {
+      FEGPU_CUDA(cudaMemcpyAsync(dm->n2e_elem.p, elem.data(), sizeof(int32_t) * elem.size(),
+                                 cudaMemcpyHostToDevice, s));
+      FEGPU_CUDA(cudaMemcpyAsync(dm->n2e_loc.p, loc.data(), loc.size(), cudaMemcpyHostToDevice,
+                                 s));
+    }
+    const int64_t np = E * nne * nne;
+    dm->pos_orig.alloc(sizeof(uint16_t) * std::max<int64_t>(np, 1));
+    if (np > 0) {
+      const int grid = static_cast<int>(std::min<int64_t>((np + 255) / 256, 1 << 20));
+      k_unsort_pos<<<grid, 256, 0, s>>>(dm->pos.as<uint16_t>(), fm->perm.as<int32_t>(), E,
+                                        nne * nne, dm->pos_orig.as<uint16_t>());
+      FEGPU_CUDA(cudaGetLastError());
+      ctx->launches++;
+    }
+    FEGPU_CUDA(cudaStreamSynchronize(s));  // the host vectors leave scope
+    dm->lists_ready = true;
+  }
+  if (elem_out) elem_out->swap(elem);
+}
+
+// Chunk plan for chunks of `chunk` elements: a node is gathered right after
+// the chunk holding its last incident element; `order` lists the nodes by
+// that chunk (ranges in chunk_nodes); span is the largest chunk distance
+// between a node's first and last element; the ring holds span + 2 chunks
+// (the chunks one gather reads, plus the one the next element tiles write).
+void plan_chunks(const fegpu_dofmap *dm, int64_t chunk, std::vector<int64_t> &chunk_nodes,
+                 std::vector<int32_t> &order, int &span_out, int &ring_out) {
+  const int64_t E = dm->femm->nelem;
+  const int64_t N = static_cast<int64_t>(dm->node_first.size());
+  const int64_t nch = (E + chunk - 1) / chunk;
   std::vector<int64_t> cnt(nch + 1, 0);
   int64_t span = 0;
   for (int64_t n = 0; n < N; ++n) {
-    if (ptr[n + 1] == ptr[n]) continue;
-    const int64_t cmin = elem[ptr[n]] / dm->chunk, cmaxc = elem[ptr[n + 1] - 1] / dm->chunk;
+    if (dm->node_first[n] < 0) continue;
+    const int64_t cmin = dm->node_first[n] / chunk, cmaxc = dm->node_last[n] / chunk;
     span = std::max(span, cmaxc - cmin);
     cnt[cmaxc + 1]++;
   }
   for (int64_t c = 0; c < nch; ++c) cnt[c + 1] += cnt[c];
-  dm->chunk_nodes = cnt;
   std::vector<int64_t> at(cnt.begin(), cnt.end() - 1);
-  std::vector<int32_t> order(cnt[nch]);
+  order.assign(nch > 0 ? cnt[nch] : 0, 0);
   for (int64_t n = 0; n < N; ++n) {
-    if (ptr[n + 1] == ptr[n]) continue;
-    order[at[elem[ptr[n + 1] - 1] / dm->chunk]++] = static_cast<int32_t>(n);
+    if (dm->node_first[n] < 0) continue;
+    order[at[dm->node_last[n] / chunk]++] = static_cast<int32_t>(n);
   }
-  // ring: the chunks a gather reads (span + 1) plus one, so the element tiles
-  // of the next chunk can be written while a gather still reads the ring
-  dm->span = static_cast<int>(span);
+  chunk_nodes = cnt;
+  span_out = static_cast<int>(span);
   // (at least one slot: a mesh without elements has no chunk but keeps the
   // per-slot events and slot arithmetic defined)
-  dm->ring = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(span + 2, nch)));
+  ring_out = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(span + 2, nch)));
+}
+
+// The mixed path's plan: node lists, chunks of ~24 MB of FP32 blocks (at
+// least 1024 elements), ring slots of the incident elements, the FP32 ring.
+void build_gather_plan(fegpu_dofmap *dm, int block_values) {
+  fegpu_femm *fm = dm->femm;
+  cudaStream_t s = fm->ctx->stream;
+  const int64_t E = fm->nelem;
+  std::vector<int32_t> elem;
+  build_node_lists(dm, &elem);
+  const int64_t per_elem = static_cast<int64_t>(block_values) * 4;
+  dm->chunk = std::max<int64_t>(1024, (24ll << 20) / std::max<int64_t>(per_elem, 1));
+  dm->chunk = std::min<int64_t>(dm->chunk, std::max<int64_t>(E, 1));
+  std::vector<int32_t> order;
+  plan_chunks(dm, dm->chunk, dm->chunk_nodes, order, dm->span, dm->ring);
+  std::vector<int32_t> slot(elem.size());
   for (size_t q = 0; q < elem.size(); ++q) {
     const int64_t ce = elem[q] / dm->chunk;
     slot[q] = static_cast<int32_t>((ce % dm->ring) * dm->chunk + (elem[q] - ce * dm->chunk));
@@ -153,28 +199,11 @@ void build_gather_plan(fegpu_dofmap *dm, int block_values) {
   if (!slot.empty())
     FEGPU_CUDA(cudaMemcpyAsync(dm->n2e_slot.p, slot.data(), sizeof(int32_t) * slot.size(),
                                cudaMemcpyHostToDevice, s));
-  dm->n2e_ptr.alloc(sizeof(int64_t) * (N + 1));
-  dm->n2e_elem.alloc(sizeof(int32_t) * elem.size());
-  dm->n2e_loc.alloc(loc.size());
   dm->gnodes.alloc(sizeof(int32_t) * std::max<size_t>(order.size(), 1));
-  FEGPU_CUDA(cudaMemcpyAsync(dm->n2e_ptr.p, ptr.data(), sizeof(int64_t) * (N + 1),
-                             cudaMemcpyHostToDevice, s));
-  FEGPU_CUDA(cudaMemcpyAsync(dm->n2e_elem.p, elem.data(), sizeof(int32_t) * elem.size(),
-                             cudaMemcpyHostToDevice, s));
-  FEGPU_CUDA(cudaMemcpyAsync(dm->n2e_loc.p, loc.data(), loc.size(), cudaMemcpyHostToDevice, s));
   if (!order.empty())
     FEGPU_CUDA(cudaMemcpyAsync(dm->gnodes.p, order.data(), sizeof(int32_t) * order.size(),
                                cudaMemcpyHostToDevice, s));
   dm->ke.alloc(sizeof(float) * static_cast<size_t>(dm->ring) * dm->chunk * block_values);
-  const int64_t np = E * nne * nne;
-  dm->pos_orig.alloc(sizeof(uint16_t) * std::max<int64_t>(np, 1));
-  if (np > 0) {
-    const int grid = static_cast<int>(std::min<int64_t>((np + 255) / 256, 1 << 20));
-    k_unsort_pos<<<grid, 256, 0, s>>>(dm->pos.as<uint16_t>(), fm->perm.as<int32_t>(), E, nne * nne,
-                                      dm->pos_orig.as<uint16_t>());
-    FEGPU_CUDA(cudaGetLastError());
-    ctx->launches++;
-  }
   FEGPU_CUDA(cudaStreamSynchronize(s));
   dm->gather_ready = true;
 }

@@ -52,9 +52,20 @@ extern "C" {
                                   /* isotropic elasticity                     */
 
 /* arithmetic of the element kernels */
-#define FEGPU_FP64 0   /* plain FP64 throughout                               */
+#define FEGPU_FP64 0   /* FP64 in the reference's own operation order: for    */
+                       /* bilform_diffusion and bilform_lin_elastic the       */
+                       /* matrix equals the reference algorithm's bit for     */
+                       /* bit (element arithmetic without FMA contraction,    */
+                       /* sums in element order, S + S' completion), so the   */
+                       /* exact zeros makematrix! leaves out are the same     */
 #define FEGPU_MIXED 1  /* FP32 bulk (FP64 geometry for distorted elements,    */
                        /* FP64 global accumulation)                           */
+#define FEGPU_FP64_FAST 2 /* FP64 with fused multiply-adds and Gram-sum       */
+                       /* element blocks, colour-ordered sums: within         */
+                       /* 1e-12 |K_ij| + 1e-14 max_k |K_ik| of FEGPU_FP64,    */
+                       /* several times faster; entries the reference forms   */
+                       /* by exact cancellation may come out as ~1e-17        */
+                       /* residues instead of exact zeros                     */
 
 typedef struct fegpu_context fegpu_context;
 typedef struct fegpu_femm fegpu_femm;
@@ -132,6 +143,12 @@ int fegpu_dofmap_copy_pattern(fegpu_dofmap *dm, int64_t *colptr, int64_t *rowval
  * (src/AssemblyModule.jl:88-583): values live in the dofmap's CSR pattern. */
 int fegpu_matrix_create(fegpu_dofmap *dm, fegpu_matrix **out);
 int fegpu_matrix_destroy(fegpu_matrix *K);
+/* The assembler the matrix stands for: symmetric = 1 (the default)
+ * SysmatAssemblerSparseSymm, 0 SysmatAssemblerSparse
+ * (src/AssemblyModule.jl:88-329, 454-583).  The FEGPU_FP64 forms group their
+ * sums as that assembler does (S + S' of the lower-triangle triples, or S of
+ * all triples), which decides the last bits of the values. */
+int fegpu_matrix_set_symmetric_assembly(fegpu_matrix *K, int symmetric);
 
 /* The forms.  Each one zeroes K and assembles every element into it with the
  * deterministic colour-ordered scatter.

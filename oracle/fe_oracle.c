@@ -922,8 +922,10 @@ orc_matrix *orc_bilform(const orc_problem *p, int form, const orc_coef *c, int m
   double *Ns = (double *)malloc(sizeof(double) * npts * nne);
   double *dNs = (double *)malloc(sizeof(double) * npts * nne * mdim);
   for (int q = 0; q < npts; ++q) {
-    orc_bfun(p->etype, p->pc + q * mdim, Ns + q * nne);
-    orc_bfundpar(p->etype, p->pc + q * mdim, dNs + q * nne * mdim);
+    if (p->Ns) memcpy(Ns + q * nne, p->Ns + q * nne, sizeof(double) * nne);
+    else orc_bfun(p->etype, p->pc + q * mdim, Ns + q * nne);
+    if (p->dNs) memcpy(dNs + q * nne * mdim, p->dNs + q * nne * mdim, sizeof(double) * nne * mdim);
+    else orc_bfundpar(p->etype, p->pc + q * mdim, dNs + q * nne * mdim);
   }
   double *X = (double *)malloc(sizeof(double) * nne * sdim);
   double *Ke = (double *)malloc(sizeof(double) * n * n);
@@ -1056,8 +1058,10 @@ orc_matrix *orc_bilform_convection(const orc_problem *p, const double *vel, int 
   double *Ns = (double *)malloc(sizeof(double) * npts * nne);
   double *dNs = (double *)malloc(sizeof(double) * npts * nne * mdim);
   for (int q = 0; q < npts; ++q) {
-    orc_bfun(p->etype, p->pc + q * mdim, Ns + q * nne);
-    orc_bfundpar(p->etype, p->pc + q * mdim, dNs + q * nne * mdim);
+    if (p->Ns) memcpy(Ns + q * nne, p->Ns + q * nne, sizeof(double) * nne);
+    else orc_bfun(p->etype, p->pc + q * mdim, Ns + q * nne);
+    if (p->dNs) memcpy(dNs + q * nne * mdim, p->dNs + q * nne * mdim, sizeof(double) * nne * mdim);
+    else orc_bfundpar(p->etype, p->pc + q * mdim, dNs + q * nne * mdim);
   }
   double *X = (double *)malloc(sizeof(double) * nne * sdim);
   double *U = (double *)malloc(sizeof(double) * nne * nsd);
@@ -1115,8 +1119,10 @@ orc_matrix *orc_bilform_masslike(const orc_problem *p, const orc_coef *c, int m)
   double *Ns = (double *)malloc(sizeof(double) * npts * nne);
   double *dNs = (double *)malloc(sizeof(double) * npts * nne * mdim);
   for (int q = 0; q < npts; ++q) {
-    orc_bfun(p->etype, p->pc + q * mdim, Ns + q * nne);
-    orc_bfundpar(p->etype, p->pc + q * mdim, dNs + q * nne * mdim);
+    if (p->Ns) memcpy(Ns + q * nne, p->Ns + q * nne, sizeof(double) * nne);
+    else orc_bfun(p->etype, p->pc + q * mdim, Ns + q * nne);
+    if (p->dNs) memcpy(dNs + q * nne * mdim, p->dNs + q * nne * mdim, sizeof(double) * nne * mdim);
+    else orc_bfundpar(p->etype, p->pc + q * mdim, dNs + q * nne * mdim);
   }
   double *X = (double *)malloc(sizeof(double) * nne * sdim);
   double *Me = (double *)malloc(sizeof(double) * ndn * nc);
@@ -1166,8 +1172,10 @@ int orc_linform_dot(const orc_problem *p, const orc_coef *f, int m, double *F) {
   double *Ns = (double *)malloc(sizeof(double) * npts * nne);
   double *dNs = (double *)malloc(sizeof(double) * npts * nne * mdim);
   for (int q = 0; q < npts; ++q) {
-    orc_bfun(p->etype, p->pc + q * mdim, Ns + q * nne);
-    orc_bfundpar(p->etype, p->pc + q * mdim, dNs + q * nne * mdim);
+    if (p->Ns) memcpy(Ns + q * nne, p->Ns + q * nne, sizeof(double) * nne);
+    else orc_bfun(p->etype, p->pc + q * mdim, Ns + q * nne);
+    if (p->dNs) memcpy(dNs + q * nne * mdim, p->dNs + q * nne * mdim, sizeof(double) * nne * mdim);
+    else orc_bfundpar(p->etype, p->pc + q * mdim, dNs + q * nne * mdim);
   }
   double *X = (double *)malloc(sizeof(double) * nne * sdim);
   double *Fe = (double *)malloc(sizeof(double) * nne * ndn);

@@ -54,6 +54,11 @@ typedef struct {
   const double *rm;       /* material frame: constant 3x3 rotation matrix,  */
                           /* row-major (CSys csmat), or NULL = identity     */
   int axisymmetric;       /* IntegDomain(..., axisymmetric = true)          */
+  /* integrationdata() tables handed over by the caller (npts x nne and      */
+  /* npts x nne x mdim, row-major), as the reference's forms take them from  */
+  /* the FESet; NULL: computed here by bfun / bfundpar                       */
+  const double *Ns;
+  const double *dNs;
 } orc_problem;
 
 typedef struct {

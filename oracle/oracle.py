@@ -44,6 +44,7 @@ class _Problem(C.Structure):
         ("ndn", C.c_int), ("dofnums", C.c_void_p), ("nalldofs", C.c_int64),
         ("npts", C.c_int), ("pc", C.c_void_p), ("w", C.c_void_p),
         ("otherdim", C.c_double), ("rm", C.c_void_p), ("axisymmetric", C.c_int),
+        ("Ns", C.c_void_p), ("dNs", C.c_void_p),
     ]
 
 
@@ -269,7 +270,7 @@ class Assembler:
 
 
 def _problem(etype, conn, xyz, dofnums, nalldofs, pc, w, otherdim, keep, rm=None,
-             axisymmetric=False):
+             axisymmetric=False, tables=None):
     conn = np.ascontiguousarray(conn, dtype=np.int64)
     xyz = np.ascontiguousarray(xyz, dtype=np.float64)
     dofnums = np.ascontiguousarray(dofnums, dtype=np.int64)
@@ -283,9 +284,17 @@ def _problem(etype, conn, xyz, dofnums, nalldofs, pc, w, otherdim, keep, rm=None
         rm = np.ascontiguousarray(rm, dtype=np.float64).reshape(3, 3)
         keep.append(rm)
         rmp = _p(rm)
+    nsp = dnp = None
+    if tables is not None:
+        Ns = np.ascontiguousarray(tables[0], dtype=np.float64)
+        dN = np.ascontiguousarray(tables[1], dtype=np.float64)
+        if Ns.size != len(w) * NNE.get(etype, 2) or dN.size != Ns.size * MDIM.get(etype, 1):
+            raise ValueError("tables: npts x nne and npts x nne x mdim expected")
+        keep += [Ns, dN]
+        nsp, dnp = _p(Ns), _p(dN)
     return _Problem(etype, conn.shape[0], _p(conn), xyz.shape[0], xyz.shape[1], _p(xyz),
                     dofnums.shape[1], _p(dofnums), int(nalldofs), len(w), _p(pc), _p(w),
-                    float(otherdim), rmp, int(bool(axisymmetric)))
+                    float(otherdim), rmp, int(bool(axisymmetric)), nsp, dnp)
 
 
 def _coef(kind, data, keep):
@@ -303,14 +312,17 @@ def _coef(kind, data, keep):
 
 def bilform(form, etype, conn, xyz, dofnums, nalldofs, pc, w, coef, coef_kind=COEF_CONST,
             otherdim=1.0, m=3, symmetric=True, phases=False, asm=None, rm=None,
-            axisymmetric=False):
+            axisymmetric=False, tables=None):
     """One bilinear form, assembled like the reference's 4/5-argument call.
 
+    tables = (Ns, dN): the integrationdata() basis tables the caller hands
+    over (as the GPU library receives them); None computes them here.
     Returns the scipy CSC matrix (and, optionally, the number of exact zeros
     dropped by the symmetric completion and the phase timings).
     """
     keep = []
-    P = _problem(etype, conn, xyz, dofnums, nalldofs, pc, w, otherdim, keep, rm, axisymmetric)
+    P = _problem(etype, conn, xyz, dofnums, nalldofs, pc, w, otherdim, keep, rm, axisymmetric,
+                 tables)
     Cf = _coef(coef_kind, coef, keep)
     ph = np.zeros(3)
     kind = asm if asm is not None else (ASM_SPARSE_SYMM if symmetric else ASM_SPARSE)

@@ -1,6 +1,10 @@
 """GPU parity: libfegpu (through its C ABI) against the CPU oracle.
 
-Bar (FP64): the CSR structure is bit-exact; every value satisfies
+Bar of the reference-order FP64 path (precision "fp64", the default) for
+bilform_diffusion and bilform_lin_elastic: the matrix equals the oracle's bit
+for bit -- structure, values and the exact zeros S + S' leaves out.
+Bar of the other FP64 paths ("fp64_fast" and the remaining forms): the CSR
+structure is bit-exact; every value satisfies
     |K_ij - Kref_ij| <= 1e-12 |Kref_ij| + 1e-14 max_k |Kref_ik|
 and |(K - Kref) x| <= 1e-12 |Kref x|.  The absolute term covers entries
 formed by cancellation (mathematically zero or nearly so, e.g. vertex /
@@ -32,6 +36,19 @@ def _rowmax(K):
 
 RTOL = 1e-12
 ATOL_ROW = 1e-14
+
+
+def bitwise(K, Kr):
+    """The GPU matrix equals the oracle's bit for bit (structure and values)."""
+    K = K.tocsc()
+    R = Kr.tocsc()
+    K.sort_indices()
+    R.sort_indices()
+    assert np.array_equal(K.indptr, R.indptr), "column pointers differ from the oracle's"
+    assert np.array_equal(K.indices, R.indices), "row indices differ from the oracle's"
+    diff = np.flatnonzero(K.data.view(np.int64) != R.data.view(np.int64))
+    assert diff.size == 0, (f"{diff.size} values differ from the oracle's bitwise "
+                            f"(first: {K.data[diff[0]]!r} vs {R.data[diff[0]]!r})")
 
 
 def compare(K, Kr, tol=RTOL, structure=True, atol_row=ATOL_ROW):
@@ -67,11 +84,13 @@ def compare(K, Kr, tol=RTOL, structure=True, atol_row=ATOL_ROW):
 
 
 def _oracle_form(O, femm, form, geom, u, coef, kind=0, m=3, symmetric=True):
+    """The oracle's form on the same inputs the GPU library receives,
+    integrationdata() tables included."""
     fes = femm.integdomain.fes
     npts, Ns, dN, w, pc = femm.integdomain.integrationdata()
     return O.bilform(form, fes.code, fes.conn, geom.values, u.dofnums, u.nalldofs(), pc, w, coef,
                      coef_kind=kind, otherdim=femm.integdomain.otherdimension, m=m,
-                     symmetric=symmetric)
+                     symmetric=symmetric, tables=(Ns, dN))
 
 
 def _field(ft, n, ndn):
@@ -83,7 +102,8 @@ def _field(ft, n, ndn):
                                        ("T4", 3, ("T", 1)), ("T10", 3, ("T", 4)),
                                        ("H8", 3, ("G", 3, 3)), ("T10", 2, ("T", 5))])
 @pytest.mark.parametrize("coef", ["iso", "general", "per_element"])
-def test_diffusion_fp64(ft, O, et, n, rule, coef):
+@pytest.mark.parametrize("prec", ["fp64", "fp64_fast"])
+def test_diffusion_fp64(ft, O, et, n, rule, coef, prec):
     gen = {"H8": ft.H8block, "H20": ft.H20block, "T4": ft.T4block, "T10": ft.T10block}[et]
     fens, fes = gen(1.0, 1.2, 0.9, n, n + 1, n)
     fens.xyz = ft.meshes.jitter_interior(fens.xyz, (n, n + 1, n), 0.2, 11, box=(1.0, 1.2, 0.9))
@@ -102,19 +122,26 @@ def test_diffusion_fp64(ft, O, et, n, rule, coef):
     else:
         v = np.random.default_rng(3).lognormal(0, 1, fes.count())
         cf, oc, kind = ft.ElementwiseData(v), v.reshape(-1, 1), 1
-    K = ft.bilform_diffusion(femm, ft.SysmatAssemblerGPU(symmetric=False), geom, u, cf)
+    K = ft.bilform_diffusion(femm, ft.SysmatAssemblerGPU(symmetric=False, precision=prec), geom,
+                             u, cf)
     Kr = _oracle_form(O, femm, O.DIFFUSION, geom, u, oc, kind, symmetric=False)
     compare(K, Kr)
     assert abs(K - K.T).max() == 0.0
-    Ks = ft.bilform_diffusion(femm, geom, u, cf)
-    compare(Ks, _oracle_form(O, femm, O.DIFFUSION, geom, u, oc, kind), structure=False)
+    Ksr = _oracle_form(O, femm, O.DIFFUSION, geom, u, oc, kind)
+    if prec == "fp64":
+        bitwise(K, Kr)
+        bitwise(ft.bilform_diffusion(femm, geom, u, cf), Ksr)  # the 4-argument form
+    else:
+        Ks = ft.bilform_diffusion(femm, ft.SysmatAssemblerGPU(precision=prec), geom, u, cf)
+        compare(Ks, Ksr, structure=False)
 
 
 # ---------------------------------------------------------------- elasticity
 @pytest.mark.parametrize("et,n,rule", [("H8", 3, ("G", 3, 2)), ("H20", 2, ("G", 3, 3)),
                                        ("T4", 3, ("T", 1)), ("T10", 3, ("T", 4))])
 @pytest.mark.parametrize("coef", ["iso_const", "aniso_const", "per_element_iso", "per_element_D"])
-def test_elasticity_fp64(ft, O, et, n, rule, coef):
+@pytest.mark.parametrize("prec", ["fp64", "fp64_fast"])
+def test_elasticity_fp64(ft, O, et, n, rule, coef, prec):
     gen = {"H8": ft.H8block, "H20": ft.H20block, "T4": ft.T4block, "T10": ft.T10block}[et]
     fens, fes = gen(1.0, 1.0, 1.0, n, n, n)
     fens.xyz = ft.meshes.jitter_interior(fens.xyz, (n, n, n), 0.15, 5)
@@ -145,13 +172,19 @@ def test_elasticity_fp64(ft, O, et, n, rule, coef):
             Ds.append(A @ A.T + 6 * np.eye(6))
         oc = np.stack(Ds).reshape(-1, 36)
         cf, kind = ft.ElementwiseData(oc), 1
-    K = ft.bilform_lin_elastic(femm, ft.SysmatAssemblerGPU(symmetric=False), geom, u,
-                               ft.DeforModelRed3D, cf)
+    K = ft.bilform_lin_elastic(femm, ft.SysmatAssemblerGPU(symmetric=False, precision=prec),
+                               geom, u, ft.DeforModelRed3D, cf)
     Kr = _oracle_form(O, femm, O.LIN_ELASTIC, geom, u, oc, kind, symmetric=False)
     compare(K, Kr)
     assert abs(K - K.T).max() == 0.0
-    Ks = ft.bilform_lin_elastic(femm, geom, u, ft.DeforModelRed3D, cf)
-    compare(Ks, _oracle_form(O, femm, O.LIN_ELASTIC, geom, u, oc, kind), structure=False)
+    Ksr = _oracle_form(O, femm, O.LIN_ELASTIC, geom, u, oc, kind)
+    if prec == "fp64":
+        bitwise(K, Kr)
+        bitwise(ft.bilform_lin_elastic(femm, geom, u, ft.DeforModelRed3D, cf), Ksr)
+    else:
+        Ks = ft.bilform_lin_elastic(femm, ft.SysmatAssemblerGPU(precision=prec), geom, u,
+                                    ft.DeforModelRed3D, cf)
+        compare(Ks, Ksr, structure=False)
 
 
 # ---------------------------------------------------------------- convection
@@ -479,18 +512,49 @@ def test_connection_matrix_degree(ft, kats):
     assert deg.max() == k["max_degree"] and deg.min() == k["min_degree"]
 
 
-def test_zero_dropping_on_regular_mesh(ft, O):
-    """On a regular block exact zeros appear; symmetric semantics drop the ones
-    the oracle's S + S' drops when the values agree bitwise, and the
-    structural (keep-zeros) result matches the oracle's sparse() pattern."""
-    fens, fes = ft.H8block(1.0, 1.0, 1.0, 3, 3, 3)
-    femm = ft.FEMMBase(ft.IntegDomain(fes, ft.GaussRule(3, 2)))
+def _gpu_dropped(ft, femm, geom, u, form, cf):
+    """(exported symmetric matrix, number of exact zeros it left out)."""
+    asm = ft.SysmatAssemblerGPU(result="device")
+    if form == "diffusion":
+        M = ft.bilform_diffusion(femm, asm, geom, u, cf)
+    else:
+        M = ft.bilform_lin_elastic(femm, asm, geom, u, ft.DeforModelRed3D, cf)
+    return M.to_scipy(), M.nnz(drop_zeros=False) - M.nnz(drop_zeros=True)
+
+
+@pytest.mark.parametrize("case", ["h8_regular_diffusion", "t10_boundary_elasticity"])
+def test_zero_dropping_on_regular_mesh(ft, O, case):
+    """Meshes on which the reference's S + S' step (src/AssemblyModule.jl:576)
+    meets exact zeros: a regular H8 block (the edge couplings of a cube
+    element cancel exactly) and a T10 block whose boundary nodes stay on the
+    block faces (the benchmark jitter).  The default symmetric assembler
+    (SysmatAssemblerSparseSymm, reference-order FP64) leaves out exactly the
+    entries the oracle leaves out, and the result equals the oracle's bit for
+    bit; the structural result (SysmatAssemblerSparse) keeps them."""
+    if case == "h8_regular_diffusion":
+        fens, fes = ft.H8block(1.0, 1.0, 1.0, 3, 3, 3)
+        femm = ft.FEMMBase(ft.IntegDomain(fes, ft.GaussRule(3, 2)))
+        u = _field(ft, fens.count(), 1)
+        form, cf, oc, ofm = "diffusion", ft.DataCache(1.0), np.array([1.0]), O.DIFFUSION
+    else:
+        fens, fes = ft.t10_elastic_mesh(n=6, seed=2)
+        femm = ft.FEMMBase(ft.IntegDomain(fes, ft.TetRule(4)))
+        u = _field(ft, fens.count(), 3)
+        D = ft.isotropic_D(210e9, 0.3)
+        form, cf, oc, ofm = "elasticity", ft.DataCache(D), D, O.LIN_ELASTIC
     geom = ft.NodalField(fens.xyz)
-    u = _field(ft, fens.count(), 1)
-    K = ft.bilform_diffusion(femm, ft.SysmatAssemblerGPU(symmetric=False), geom, u,
-                             ft.DataCache(1.0))
-    Kr = _oracle_form(O, femm, O.DIFFUSION, geom, u, np.array([1.0]), symmetric=False)
-    compare(K, Kr)
+    npts, Ns, dN, w, pc = femm.integdomain.integrationdata()
+    Kr, dropped, _ = O.bilform(ofm, fes.code, fes.conn, geom.values, u.dofnums, u.nalldofs(), pc,
+                               w, oc, phases=True, tables=(Ns, dN))
+    assert dropped > 0, "the mesh should meet exact zeros"
+    K, gpu_dropped = _gpu_dropped(ft, femm, geom, u, form, cf)
+    assert gpu_dropped == dropped
+    bitwise(K, Kr)
+    Kn = (ft.bilform_diffusion(femm, ft.SysmatAssemblerGPU(symmetric=False), geom, u, cf)
+          if form == "diffusion" else
+          ft.bilform_lin_elastic(femm, ft.SysmatAssemblerGPU(symmetric=False), geom, u,
+                                 ft.DeforModelRed3D, cf))
+    bitwise(Kn, _oracle_form(O, femm, ofm, geom, u, oc, symmetric=False))
 
 
 @pytest.mark.parametrize("et", ["H8", "T10", "H20"])
