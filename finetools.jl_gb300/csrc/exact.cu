@@ -13,6 +13,7 @@
 // reference's sparse `+` leaves them out.
 #include <algorithm>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -23,6 +24,9 @@ namespace fegpu {
 namespace {
 
 constexpr int kExactGatherWarps = 8;
+}  // namespace
+int exact_tile(int etype, int form, int npts);
+namespace {
 
 // doubles of shared memory per warp: the node's NDN rows, one or two buckets
 __host__ __device__ inline int exact_warp_stride(int ndn, int maxdeg, bool sym) {
@@ -164,15 +168,28 @@ int launch_exact(int etype, int form, const KArgs &a, int num_sms, cudaStream_t 
   throw Error{FEGPU_ERR_ARG, "unknown element type"};
 }
 
-// chunks of ~16 MB of FP64 blocks (at least 256 elements); the ring of span +
-// 2 chunks then stays near the size of the L2
-void build_exact_plan(fegpu_dofmap *dm, int block_values) {
+// CTAs of the block kernel resident per SM (shared memory; registers allow
+// four of 256 threads)
+int exact_ctas_per_sm(int etype, int form, int npts, int te) {
+  const size_t smem = exact_layout(nodes_per_elem(etype), manif_dim(etype), npts, te, form).total;
+  return static_cast<int>(std::max<size_t>(1, std::min<size_t>(4, (228 * 1024) / (smem + 1024))));
+}
+
+// Chunks of four waves of element tiles over the GPU (at least 256
+// elements): the block kernel is FP64-bound, and a chunk of fewer tiles than
+// CTA slots leaves SMs idle while it runs (one 16 MB chunk of T10 blocks, 163
+// tiles on 304 slots: FP64 pipe 79 % busy on the active SMs, 43 % over the
+// launch).  The ring of span + 2 chunks then exceeds the L2, which this
+// compute-bound path does not need.
+void build_exact_plan(fegpu_dofmap *dm, int block_values, int form) {
   fegpu_femm *fm = dm->femm;
   cudaStream_t s = fm->ctx->stream;
   const int64_t E = fm->nelem;
   build_node_lists(dm, nullptr);
-  const int64_t per_elem = static_cast<int64_t>(block_values) * 8;
-  dm->x_chunk = std::max<int64_t>(256, (16ll << 20) / std::max<int64_t>(per_elem, 1));
+  const int te = exact_tile(fm->etype, form, fm->npts);
+  const int64_t slots =
+      static_cast<int64_t>(fm->ctx->num_sms) * exact_ctas_per_sm(fm->etype, form, fm->npts, te);
+  dm->x_chunk = std::max<int64_t>(256, 4 * slots * te);
   dm->x_chunk = std::min<int64_t>(dm->x_chunk, std::max<int64_t>(E, 1));
   std::vector<int32_t> order;
   plan_chunks(dm, dm->x_chunk, dm->x_chunk_nodes, order, dm->x_span, dm->x_ring);
@@ -198,6 +215,15 @@ int exact_tile(int etype, int form, int npts) {
   const size_t budget = per > 24 * 1024 ? 220 * 1024 : 110 * 1024;
   int te = static_cast<int>((budget - std::min(budget, fixed)) / std::max<size_t>(per, 1));
   te = std::max(1, std::min(te, 64));
+  // FEGPU_EXACT_TILE fixes the elements per tile (tuning; capped by the
+  // shared memory of one CTA)
+  if (const char *env = std::getenv("FEGPU_EXACT_TILE")) {
+    const int v = std::atoi(env);
+    if (v > 0) {
+      te = v;
+      while (te > 1 && exact_layout(nne, mdim, npts, te, form).total > 227 * 1024) --te;
+    }
+  }
   FEGPU_REQUIRE(exact_layout(nne, mdim, npts, te, form).total <= 227 * 1024,
                 "quadrature rule too large for the reference-order element kernel");
   return te;
@@ -210,9 +236,15 @@ void run_exact(fegpu_dofmap *dm, int form, KArgs &a, bool symmetric) {
   fegpu_context *ctx = fm->ctx;
   const int nne = fm->nne, ndn = dm->ndn;
   const int bs = ndn * ndn, nblk = nne * (nne + 1) / 2;
-  if (!dm->exact_ready) build_exact_plan(dm, nblk * bs);
+  // the plan depends on the tile (chunks are waves of tiles): rebuilt when
+  // another form or rule changes it
+  const int te = exact_tile(fm->etype, form, fm->npts);
+  if (!dm->exact_ready || dm->x_tile != te) {
+    build_exact_plan(dm, nblk * bs, form);
+    dm->x_tile = te;
+  }
   a.conn = fm->conn_orig.as<int32_t>();
-  a.te = exact_tile(fm->etype, form, fm->npts);
+  a.te = te;
   GArgs g;
   std::memset(&g, 0, sizeof(g));
   g.n2e_ptr = dm->n2e_ptr.as<int64_t>();

@@ -156,7 +156,7 @@ struct fegpu_dofmap {
   // node-to-element lists, and an FP64 block ring
   bool exact_ready = false;
   int64_t x_chunk = 0;
-  int x_ring = 0, x_span = 0;
+  int x_ring = 0, x_span = 0, x_tile = 0;
   std::vector<int64_t> x_chunk_nodes;
   fegpu::DevBuf x_gnodes;   // int32: nodes in gather order
   fegpu::DevBuf x_ke;       // double ring of element blocks

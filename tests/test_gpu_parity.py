@@ -24,6 +24,30 @@ pytestmark = pytest.mark.gpu
 MIXED_TOL = 1e-6
 
 
+def mixed_gate(K32, K64, tol=MIXED_TOL, seed=5):
+    """The mixed-precision error gate against FP64, per nonzero and normwise:
+        max_ij |dK_ij| / max_k |K_ik| <= tol   (the row's scale)
+        |dK x| / |K x| <= tol                  (x uniform in [-1, 1])
+    A raw per-entry relative bound cannot hold in FP32 for entries formed by
+    cancellation (near zero in FP64: an FP32 rounding of the row's terms is
+    larger than the entry); the row scale is what such an entry's accuracy
+    is measured against.  Returns (row-scaled, normwise)."""
+    A = K64.tocsr()
+    B = K32.tocsr()
+    rows = np.abs(A).max(axis=1).toarray().ravel()
+    D = (B - A).tocsr()
+    D.data = np.abs(D.data)
+    dr = D.max(axis=1).toarray().ravel()
+    nz = rows > 0
+    row = float((dr[nz] / rows[nz]).max()) if nz.any() else 0.0
+    assert np.all(dr[~nz] == 0)
+    x = np.random.default_rng(seed).uniform(-1, 1, A.shape[1])
+    kx = float(np.linalg.norm((B - A) @ x) / np.linalg.norm(A @ x))
+    assert row <= tol, f"row-scaled per-nonzero error {row:.3e} > {tol:g}"
+    assert kx <= tol, f"|dK x| / |K x| = {kx:.3e} > {tol:g}"
+    return row, kx
+
+
 def _rowmax(K):
     """max |K_ij| per row (0 for an empty row)."""
     R = K.tocsr()
@@ -245,6 +269,7 @@ def test_div_grad_fp64(ft, O, et, n, rule, coef):
                              geom, u, cf)
     x = rng.uniform(-1, 1, K.shape[0])
     assert np.linalg.norm((Km - K) @ x) <= MIXED_TOL * np.linalg.norm(K @ x)
+    mixed_gate(Km, K)
 
 
 # ---------------------------------------------------------------- dot / linform
@@ -403,6 +428,7 @@ def test_isolated_nodes_and_single_element(ft, O):
                                      geom, u, ft.DeforModelRed3D, ft.DataCache(D))
         x = rng.uniform(-1, 1, K.shape[0])
         assert np.linalg.norm((K32 - K) @ x) / np.linalg.norm(K @ x) <= MIXED_TOL
+        mixed_gate(K32, K)
         untouched = np.setdiff1d(np.arange(1, n + 1), np.unique(conn))
         rows = u.dofnums[untouched - 1].ravel() - 1
         assert abs(K.tocsr()[rows]).sum() == 0 and abs(K32.tocsr()[rows]).sum() == 0
@@ -714,6 +740,7 @@ def test_mixed_precision(ft, O, et):
     x = rng.uniform(-1, 1, K64.shape[0])
     assert np.linalg.norm((K32 - K64) @ x) / np.linalg.norm(K64 @ x) <= MIXED_TOL
     assert abs(K32 - K64).max() / abs(K64).max() <= MIXED_TOL
+    mixed_gate(K32, K64)
     assert abs(K32 - K32.T).max() == 0.0
 
 
@@ -744,6 +771,7 @@ def test_mixed_t10_straight_and_curved(ft, O, curved):
     x = rng.uniform(-1, 1, K64.shape[0])
     assert np.linalg.norm((K32 - K64) @ x) / np.linalg.norm(K64 @ x) <= MIXED_TOL
     assert abs(K32 - K64).max() / abs(K64).max() <= MIXED_TOL
+    mixed_gate(K32, K64)
     assert abs(K32 - K32.T).max() == 0.0
     # the FP64 path against the oracle: corner Jacobians on the straight
     # elements, isoparametric ones on the curved
@@ -973,6 +1001,7 @@ def test_mixed_tensor_core_blocks(ft, et, monkeypatch):
         err_kx = np.linalg.norm((K - K64) @ x) / np.linalg.norm(K64 @ x)
         err_max = abs(K - K64).max() / abs(K64).max()
         assert err_kx <= MIXED_TOL and err_max <= MIXED_TOL, (flag, err_kx, err_max)
+        mixed_gate(K, K64)
         assert abs(K - K.T).max() == 0.0
     assert abs(out["1"] - out["0"]).max() > 0.0
 
@@ -1153,6 +1182,7 @@ def test_high_order_gauss_rules(ft, O, et, form, order):
                                      ft.DeforModelRed3D, ft.DataCache(D))
         x = rng.uniform(-1, 1, K.shape[0])
         assert np.linalg.norm((K32 - K) @ x) <= MIXED_TOL * np.linalg.norm(K @ x)
+        mixed_gate(K32, K)
     elif form == "diffusion":
         u = _field(ft, fens.count(), 1)
         K = ft.bilform_diffusion(femm, geom, u, ft.DataCache(1.3))
@@ -1263,3 +1293,4 @@ def test_axisymmetric_forms(ft, O, kats, form):
     compare(K, Kr)
     x = np.random.default_rng(5).uniform(-1, 1, K.shape[0])
     assert np.linalg.norm((K32 - K) @ x) <= MIXED_TOL * np.linalg.norm(K @ x)
+    mixed_gate(K32, K)
