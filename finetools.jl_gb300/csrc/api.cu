@@ -459,6 +459,13 @@ int fegpu_context_create(int device, fegpu_context **out) {
       delete ctx;
       throw Error{FEGPU_ERR_CUDA, std::string("context: ") + cudaGetErrorString(e)};
     }
+    try {
+      noalloc_prepare(device);
+    } catch (...) {
+      cudaStreamDestroy(ctx->stream);
+      delete ctx;
+      throw;
+    }
     *out = ctx;
   });
 }

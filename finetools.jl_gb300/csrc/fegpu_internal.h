@@ -289,6 +289,9 @@ KArgs base_args(fegpu_matrix *K, fegpu_dofmap *dm);
 // (on the device) for a copy of them still in flight to the host
 void await_export(fegpu_matrix *K, cudaStream_t s);
 bool is_isotropic(const double *D, double &lam, double &mu);
+// loads the allocation-free entry point's static array on the current device
+// and looks its address up (noalloc.cu); called when a context is created
+void noalloc_prepare(int device);
 
 // ---- matrix utilities -----------------------------------------------------------
 void spmv(const fegpu_dofmap *dm, const double *val, const double *x, double *y,

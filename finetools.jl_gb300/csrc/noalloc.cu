@@ -11,7 +11,8 @@
 // and calls no cudaMalloc, cudaFree or other allocating routine.
 //
 // The array has a fixed size (FEGPU_NOALLOC_SCRATCH_BYTES, 64 MiB) and every
-// GPU that loads the library holds it until the process exits.  All calls
+// GPU on which a library context is created holds it until the process exits
+// (fegpu_context_create looks its address up, which loads it).  All calls
 // share it and it keeps the last call's contents; nothing in it needs to
 // start at zero (every block, order entry and coefficient is written before
 // it is read).  Calls whose GPU work overlaps (two streams, or two host
@@ -60,6 +61,18 @@ int *status_address(int device) {
 
 size_t align256(size_t n) { return (n + 255) / 256 * 256; }
 
+}  // namespace
+
+// Called by fegpu_context_create with the device current: looking the two
+// symbols up loads this file's module, and with it the static array, before
+// the caller's own allocator reserves the GPU's memory.
+void noalloc_prepare(int device) {
+  scratch_address(device);
+  status_address(device);
+}
+
+namespace {
+
 // ring chunks needed when elements are cut in chunks of c: a node's incident
 // elements span (last / c - first / c + 1) chunks
 int ring_for(const fegpu_dofmap *dm, int64_t c) {
@@ -90,7 +103,7 @@ extern "C" int fegpu_bilform_lin_elastic_noalloc(fegpu_matrix *K, const fegpu_co
                   "run one mixed-precision assembly on this matrix first "
                   "(fegpu_bilform_lin_elastic with FEGPU_MIXED builds the node-to-element "
                   "tables this entry point reads)"};
-    void *base = scratch_address(ctx->device);  // first call on a device: symbol lookup
+    void *base = scratch_address(ctx->device);  // looked up when the context was created
     K->unsym = false;
     const int64_t E = fm->nelem;
     const int nne = fm->nne;
@@ -122,7 +135,9 @@ extern "C" int fegpu_bilform_lin_elastic_noalloc(fegpu_matrix *K, const fegpu_co
                   "per-element (lambda, mu)"};
     }
     a.coef_kind = cf->kind;
-    a.ncomp = cf->ncomp;
+    // the same kernel arguments as fegpu_bilform_lin_elastic: an isotropic
+    // constant D travels as its (lambda, mu) pair
+    a.ncomp = (form == F_ELAST_ISO && cf->kind == FEGPU_COEF_CONST) ? 2 : cf->ncomp;
 
     // chunk size: the largest (from the regular plan's down) whose ring,
     // node order and coefficients fit in the static array

@@ -236,14 +236,14 @@ int fegpu_matrix_cg(fegpu_matrix *K, const double *b, const double *x0, int maxi
  * Same arguments and result as fegpu_bilform_lin_elastic(K, cf, FEGPU_MIXED);
  * all scratch (element-block ring, node gather order, per-element
  * coefficients) lives in one static device array of
- * FEGPU_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until
+ * FEGPU_NOALLOC_SCRATCH_BYTES, which fegpu_context_create loads (and looks
+ * its device address up) on its device, so that GPU holds it from then until
  * the process exits; meshes whose scratch would not fit are rejected with an
  * error.  Calls no cudaMalloc or cudaFree.  Preconditions: one regular
- * FEGPU_MIXED assembly on the same matrix has run (it builds the node-to-element
- * tables read here).  The first call on a device looks up the array's device
- * address; make that first call before any stream capture.  Calls share the
- * array (it keeps the last call's contents): calls whose GPU work overlaps
- * race. */
+ * FEGPU_MIXED assembly on the same matrix has run (it builds the
+ * node-to-element tables read here).  The call blocks the host until its
+ * work is done.  Calls share the array (it keeps the last call's contents):
+ * calls whose GPU work overlaps race. */
 #define FEGPU_NOALLOC_SCRATCH_BYTES (64u * 1024u * 1024u)
 int fegpu_bilform_lin_elastic_noalloc(fegpu_matrix *K, const fegpu_coef *cf);
 

@@ -1,9 +1,9 @@
 """Extract the known-answer data of the reference's own tests into JSON.
 
-Run in a checkout that has the FinEtools.jl sources (default location
-``/root/reference``; override with ``FINETOOLS_REF``):
+Run with the path of a FinEtools.jl source checkout, as an argument or in
+the FINETOOLS_REF environment variable (one of them is required):
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py <path of the FinEtools.jl sources>
 
 It reads the Julia test files as text (nothing is executed), pulls out the
 literal matrices, DOF lists, mesh parameters and expected answers of the
@@ -17,7 +17,7 @@ import os
 import re
 import sys
 
-REF = os.environ.get("FINETOOLS_REF", "/root/reference")
+REF = None  # the FinEtools.jl source checkout (command line or FINETOOLS_REF)
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_kats.json")
 
 
@@ -316,6 +316,11 @@ def masslike_case():
 
 
 def main():
+    global REF
+    REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("FINETOOLS_REF")
+    if not REF:
+        sys.exit("usage: make_golden.py <path of the FinEtools.jl sources> "
+                 "(or set FINETOOLS_REF)")
     if not os.path.isdir(REF):
         sys.exit(f"reference sources not found at {REF}")
     data = {"assembler": assembler_kats(), "patch": patch_tests(), **coloring_and_pattern(),
