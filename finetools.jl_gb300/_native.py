@@ -10,7 +10,10 @@ import ctypes as C
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIBPATH = os.path.join(HERE, "libfegpu.so")
+# FEGPU_DEVICE_CHECKS=1 loads the build with device index checks
+# (build.py --device-checks)
+LIBPATH = os.path.join(HERE, "libfegpu_checked.so" if os.environ.get("FEGPU_DEVICE_CHECKS") == "1"
+                       else "libfegpu.so")
 
 OK = 0
 Q4, H8, H20, T4, T10 = 0, 1, 2, 3, 4
@@ -23,7 +26,7 @@ ASM_SPARSE, ASM_SPARSE_SYMM, ASM_SPARSE_DIAG, ASM_HRZ_LUMPING_SYMM = 0, 1, 2, 3
 EXPORTS = [
     "fegpu_last_error", "fegpu_context_create", "fegpu_context_destroy",
     "fegpu_context_synchronize", "fegpu_context_stream", "fegpu_context_timing",
-    "fegpu_context_kernel_stats", "fegpu_femm_create", "fegpu_femm_destroy",
+    "fegpu_context_kernel_stats", "fegpu_context_device_checks", "fegpu_femm_create", "fegpu_femm_destroy",
     "fegpu_femm_set_geometry", "fegpu_femm_set_axisymmetric", "fegpu_femm_colors", "fegpu_dofmap_create",
     "fegpu_dofmap_destroy", "fegpu_dofmap_copy_pattern", "fegpu_matrix_create",
     "fegpu_matrix_destroy", "fegpu_matrix_set_symmetric_assembly", "fegpu_bilform_diffusion", "fegpu_bilform_lin_elastic",
@@ -33,7 +36,7 @@ EXPORTS = [
     "fegpu_assembler_destroy", "fegpu_assembler_assemble", "fegpu_assembler_make",
     "fegpu_assembler_copy_csc", "fegpu_bilform_masslike", "fegpu_bilform_lin_elastic_noalloc",
     "fegpu_batch_create", "fegpu_batch_destroy", "fegpu_batch_add", "fegpu_batch_set_coef",
-    "fegpu_batch_tune", "fegpu_batch_tile", "fegpu_batch_set_wait_limit", "fegpu_batch_launch",
+    "fegpu_batch_tune", "fegpu_batch_tile", "fegpu_batch_set_wait_limit", "fegpu_batch_withhold", "fegpu_batch_launch",
     "fegpu_batch_wait", "fegpu_batch_run", "fegpu_batch_stats",
     "fegpu_server_create", "fegpu_server_destroy", "fegpu_server_add_mesh", "fegpu_server_submit",
     "fegpu_server_wait", "fegpu_server_drain", "fegpu_server_hold", "fegpu_server_stats",
@@ -72,6 +75,7 @@ def load(path: str = LIBPATH):
         "fegpu_context_stream": ([vp, pp], i32),
         "fegpu_context_timing": ([vp, i32], i32),
         "fegpu_context_kernel_stats": ([vp, C.POINTER(C.c_double), p64, i32], i32),
+        "fegpu_context_device_checks": ([vp, C.POINTER(C.c_int)], i32),
         "fegpu_femm_create": ([vp, i32, i64, vp, i64, i32, vp, vp, vp, d, pp], i32),
         "fegpu_femm_destroy": ([vp], i32),
         "fegpu_femm_set_geometry": ([vp, i32, vp], i32),
@@ -112,6 +116,7 @@ def load(path: str = LIBPATH):
         "fegpu_batch_tune": ([vp, C.c_char_p], i32),
         "fegpu_batch_tile": ([vp, i64, C.POINTER(C.c_int)], i32),
         "fegpu_batch_set_wait_limit": ([vp, d], i32),
+        "fegpu_batch_withhold": ([vp, i64], i32),
         "fegpu_batch_launch": ([vp], i32),
         "fegpu_batch_wait": ([vp], i32),
         "fegpu_batch_run": ([vp], i32),

@@ -97,6 +97,11 @@ class AssemblyBatch:
     def set_wait_limit(self, seconds: float):
         nat.check(nat.load().fegpu_batch_set_wait_limit(self.h, float(seconds)))
 
+    def withhold(self, job: int):
+        """Test of the failure path: withhold the completion of job's first
+        element stage (job = -1: none), so the waits on it run out."""
+        nat.check(nat.load().fegpu_batch_withhold(self.h, int(job)))
+
     def launch(self):
         nat.check(nat.load().fegpu_batch_launch(self.h))
 

@@ -17,6 +17,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libfegpu.so")
+LIB_CHECKED = os.path.join(HERE, "libfegpu_checked.so")
 ROOT = os.path.dirname(HERE)
 INCLUDE = os.path.join(ROOT, "include")
 
@@ -55,35 +56,42 @@ def _compile(cmd):
     return r.stderr
 
 
-def build(jobs: int | None = None, verbose: bool = False, force: bool = False) -> str:
-    os.makedirs(BUILD, exist_ok=True)
+def build(jobs: int | None = None, verbose: bool = False, force: bool = False,
+          device_checks: bool = False) -> str:
+    """Builds libfegpu.so; device_checks=True builds libfegpu_checked.so, whose
+    kernels check the indices they read and write (FEGPU_DEVICE_CHECKS)."""
+    build_dir = BUILD + ("_checked" if device_checks else "")
+    lib = LIB_CHECKED if device_checks else LIB
+    defs = ["-DFEGPU_DEVICE_CHECKS"] if device_checks else []
+    os.makedirs(build_dir, exist_ok=True)
     nvcc = _nvcc()
     deps = _headers()
     cmds, objs = [], []
     for src in sorted(glob.glob(os.path.join(CSRC, "*.cu"))):
-        obj = os.path.join(BUILD, os.path.basename(src) + ".o")
+        obj = os.path.join(build_dir, os.path.basename(src) + ".o")
         objs.append(obj)
         if force or _stale(obj, src, deps):
             extra = ["-Xptxas", "-v"] if verbose else []
-            cmds.append([nvcc] + NVCC_FLAGS + extra + ["-c", src, "-o", obj])
+            cmds.append([nvcc] + NVCC_FLAGS + defs + extra + ["-c", src, "-o", obj])
     for src in sorted(glob.glob(os.path.join(CSRC, "*.cpp"))):
-        obj = os.path.join(BUILD, os.path.basename(src) + ".o")
+        obj = os.path.join(build_dir, os.path.basename(src) + ".o")
         objs.append(obj)
         if force or _stale(obj, src, deps):
-            cmds.append(["g++"] + CXX_FLAGS + ["-c", src, "-o", obj])
+            cmds.append(["g++"] + CXX_FLAGS + defs + ["-c", src, "-o", obj])
     if cmds:
         jobs = jobs or min(len(cmds), max(1, os.cpu_count() or 1))
         with cf.ThreadPoolExecutor(jobs) as ex:
             for log in ex.map(_compile, cmds):
                 if verbose and log:
                     sys.stderr.write(log)
-    if cmds or not os.path.exists(LIB) or any(
-            os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
-        tmp = LIB + ".tmp"
+    if cmds or not os.path.exists(lib) or any(
+            os.path.getmtime(o) > os.path.getmtime(lib) for o in objs):
+        tmp = lib + ".tmp"
         _compile([nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"])
-        os.replace(tmp, LIB)
-    return LIB
+        os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":
-    print(build(verbose="-v" in sys.argv, force="-f" in sys.argv))
+    print(build(verbose="-v" in sys.argv, force="-f" in sys.argv,
+                device_checks="--device-checks" in sys.argv))

@@ -208,6 +208,22 @@ void await_export(fegpu_matrix *K, cudaStream_t s) {
   if (K && K->export_pending) FEGPU_CUDA(cudaStreamWaitEvent(s, K->exported, 0));
 }
 
+void device_checks(fegpu_context *ctx, cudaStream_t s) {
+  if (!kDeviceChecks || !ctx->check_word.p) return;
+  unsigned long long w = 0;
+  FEGPU_CUDA(cudaMemcpyAsync(&w, ctx->check_word.p, sizeof(w), cudaMemcpyDeviceToHost, s));
+  FEGPU_CUDA(cudaStreamSynchronize(s));
+  if (w == 0) return;
+  FEGPU_CUDA(cudaMemsetAsync(ctx->check_word.p, 0, sizeof(w), s));
+  static const char *const kSites[] = {"?", "node number of an element", "CSR slot of the scatter",
+                                       "CSR slot of the row gather", "vector entry"};
+  const int site = static_cast<int>(w >> 56);
+  throw Error{FEGPU_ERR_DEVICE,
+              std::string("device index check: ") + kSites[site <= 4 ? site : 0] + " " +
+                  std::to_string(static_cast<long long>(w & ((1ull << 56) - 1ull))) +
+                  " out of range (the kernel skipped the access)"};
+}
+
 KArgs base_args(fegpu_matrix *K, fegpu_dofmap *dm) {
   fegpu_femm *fm = dm->femm;
   await_export(K, fm->ctx->stream);
@@ -223,6 +239,9 @@ KArgs base_args(fegpu_matrix *K, fegpu_dofmap *dm) {
   a.colperm = dm->contiguous ? nullptr : dm->colperm.as<int32_t>();
   a.cpoff = dm->contiguous ? nullptr : dm->cpoff.as<int64_t>();
   a.val = K ? K->val.as<double>() : nullptr;
+  a.nnz = dm->nnz;
+  a.nnodes = fm->nnodes;
+  a.check = fm->ctx->check_word.as<unsigned long long>();  // null without device checks
   a.npts = fm->npts;
   a.sdim = fm->sdim;
   a.otherdim = fm->otherdim;
@@ -314,6 +333,7 @@ void run_gather(fegpu_dofmap *dm, int form, KArgs &a) {
   FEGPU_REQUIRE(tile_smem_bytes(fm->etype, form, fm->npts, a.te) <= 227 * 1024,
                 "quadrature rule too large for the element kernel");
   GArgs g;
+  std::memset(&g, 0, sizeof(g));
   g.n2e_ptr = dm->n2e_ptr.as<int64_t>();
   g.n2e_elem = dm->n2e_elem.as<int32_t>();
   g.n2e_loc = dm->n2e_loc.as<uint8_t>();
@@ -330,6 +350,8 @@ void run_gather(fegpu_dofmap *dm, int form, KArgs &a) {
   g.cpoff = dm->contiguous ? nullptr : dm->cpoff.as<int64_t>();
   g.val = a.val;
   g.maxdeg = dm->maxdeg;
+  g.check = a.check;
+  g.nnz = dm->nnz;
   const int64_t nch = static_cast<int64_t>(dm->chunk_nodes.size()) - 1;
   // Element blocks on the side stream, gathers on the context stream: the
   // blocks of chunk c wait for the gather that last read their ring slot
@@ -461,6 +483,10 @@ int fegpu_context_create(int device, fegpu_context **out) {
     }
     try {
       noalloc_prepare(device);
+      if (kDeviceChecks) {
+        ctx->check_word.alloc(sizeof(unsigned long long));
+        FEGPU_CUDA(cudaMemset(ctx->check_word.p, 0, sizeof(unsigned long long)));
+      }
     } catch (...) {
       cudaStreamDestroy(ctx->stream);
       delete ctx;
@@ -499,6 +525,13 @@ int fegpu_context_kernel_stats(fegpu_context *ctx, double *kernel_ms, int64_t *l
       ctx->kernel_ms = 0.0;
       ctx->launches = 0;
     }
+  });
+}
+
+int fegpu_context_device_checks(fegpu_context *ctx, int *enabled) {
+  return guarded([&] {
+    FEGPU_REQUIRE(ctx && enabled, "null handle");
+    *enabled = kDeviceChecks ? 1 : 0;
   });
 }
 
@@ -784,6 +817,7 @@ int fegpu_bilform_diffusion(fegpu_matrix *K, const fegpu_coef *cf, int precision
       if (fm->nelem > 0) run_form(dm, form, precision, a);
     }
     FEGPU_CUDA(cudaStreamSynchronize(fm->ctx->stream));  // st owns the staged data
+    device_checks(fm->ctx, fm->ctx->stream);
   });
 }
 
@@ -834,6 +868,7 @@ int fegpu_bilform_lin_elastic(fegpu_matrix *K, const fegpu_coef *cf, int precisi
       if (fm->nelem > 0) run_exact(dm, form, a, K->symm_asm);
       else zero_matrix(K);
       FEGPU_CUDA(cudaStreamSynchronize(fm->ctx->stream));
+      device_checks(fm->ctx, fm->ctx->stream);
       return;
     }
     const bool gather = precision == FEGPU_MIXED;
@@ -863,6 +898,7 @@ int fegpu_bilform_lin_elastic(fegpu_matrix *K, const fegpu_coef *cf, int precisi
     if (!gather) zero_matrix(K);
     if (fm->nelem > 0) run_form(dm, form, precision, a);
     FEGPU_CUDA(cudaStreamSynchronize(fm->ctx->stream));
+    device_checks(fm->ctx, fm->ctx->stream);
   });
 }
 
@@ -910,6 +946,7 @@ int fegpu_bilform_div_grad(fegpu_matrix *K, const fegpu_coef *cf, int precision)
     if (!gather) zero_matrix(K);
     if (fm->nelem > 0) run_form(dm, F_ELAST_ISO, precision, a);
     FEGPU_CUDA(cudaStreamSynchronize(fm->ctx->stream));
+    device_checks(fm->ctx, fm->ctx->stream);
   });
 }
 
@@ -962,6 +999,7 @@ int fegpu_bilform_dot(fegpu_matrix *K, const fegpu_coef *cf, int m, int symmetri
     zero_matrix(K);
     if (fm->nelem > 0) run_colours(dm, F_DOT, FEGPU_FP64, a);
     FEGPU_CUDA(cudaStreamSynchronize(fm->ctx->stream));
+    device_checks(fm->ctx, fm->ctx->stream);
   });
 }
 
@@ -984,7 +1022,9 @@ int fegpu_linform_dot(fegpu_dofmap *dm, const fegpu_coef *f, int m, double *F) {
     cudaStream_t s = fm->ctx->stream;
     FEGPU_CUDA(cudaMemsetAsync(vec.p, 0, sizeof(double) * dm->ndof, s));
     a.val = vec.as<double>();
+    a.nnz = dm->ndof;
     if (fm->nelem > 0) run_colours(dm, F_LIN, FEGPU_FP64, a);
+    device_checks(fm->ctx, s);
     FEGPU_CUDA(cudaMemcpyAsync(F, vec.p, sizeof(double) * dm->ndof, cudaMemcpyDeviceToHost, s));
     FEGPU_CUDA(cudaStreamSynchronize(s));
   });

@@ -99,11 +99,14 @@ __device__ void gather_dispatch(const BatchJob &J, int64_t b, int64_t e, unsigne
   }
 }
 
-// The persistent kernel.  status: 0 ok, 1 a wait ran out of time.
+// The persistent kernel.  status: 0 ok, 1 a wait ran out of time.  withheld
+// (>= 0): the completions of that counter are not published, so the items that
+// wait on it run out of time (the failure path, exercised by a test).
 __global__ void __launch_bounds__(kBatchThreads, 2) k_batch(const BatchJob *jobs,
                                                          const BatchItem *items, int nitems,
                                                          int *next, int *counters, int *status,
-                                                         unsigned long long wait_ns) {
+                                                         unsigned long long wait_ns,
+                                                         int withheld) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ int s_item, s_go;
   for (;;) {
@@ -148,7 +151,7 @@ __global__ void __launch_bounds__(kBatchThreads, 2) k_batch(const BatchJob *jobs
       else gather_dispatch(J, I.b, I.e, smem);
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (threadIdx.x == 0 && I.done != withheld) {
       __threadfence();  // release this item's writes
       atomicAdd(&counters[I.done], 1);
     }
@@ -191,9 +194,10 @@ const char *batch_code_name(int code) {
 
 void launch_batch_kernel(int grid, size_t smem, cudaStream_t s, const BatchJob *jobs,
                          const BatchItem *items, int nitems, int *next, int *counters,
-                         int *status, double wait_s) {
+                         int *status, double wait_s, int withheld) {
   k_batch<<<grid, kBatchThreads, smem, s>>>(jobs, items, nitems, next, counters, status,
-                                            static_cast<unsigned long long>(wait_s * 1e9));
+                                            static_cast<unsigned long long>(wait_s * 1e9),
+                                            withheld);
   FEGPU_CUDA(cudaGetLastError());
 }
 
@@ -243,6 +247,7 @@ struct fegpu_batch {
   int nitems = 0, ncounters = 0, grid = 0;
   size_t smem = 0;
   double wait_s = 5.0;                // time budget of one dependency wait
+  int withheld = -1;                  // counter whose completions are withheld (test hook)
   bool dirty = true;                  // queue and graph must be rebuilt
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -339,6 +344,8 @@ void make_batch_job(fegpu_matrix *K, int form, int code, int m, const fegpu_coef
   g.cpoff = dm->contiguous ? nullptr : dm->cpoff.as<int64_t>();
   g.val = K->val.as<double>();
   g.maxdeg = dm->maxdeg;
+  g.check = out.k.check;
+  g.nnz = dm->nnz;
   out.code = code;
   out.form = form;
   out.etype = fm->etype;
@@ -410,7 +417,7 @@ void enqueue_batch(fegpu_batch *b, cudaStream_t st) {
   FEGPU_CUDA(cudaMemsetAsync(b->d_status.p, 0, sizeof(int), st));
   launch_batch_kernel(b->grid, b->smem, st, b->d_jobs.as<BatchJob>(), b->d_items.as<BatchItem>(),
                       b->nitems, b->d_next.as<int>(), b->d_counters.as<int>(),
-                      b->d_status.as<int>(), b->wait_s);
+                      b->d_status.as<int>(), b->wait_s, b->withheld);
 }
 
 void check_status(fegpu_batch *b) {
@@ -570,6 +577,7 @@ int fegpu_batch_wait(fegpu_batch *b) {
     if (b->jobs.empty() || b->dirty) return;
     fegpu_context *ctx = b->ctx;
     check_status(b);
+    device_checks(ctx, ctx->stream);
     if (ctx->timing) {
       float ms = 0.f;
       FEGPU_CUDA(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
@@ -581,6 +589,24 @@ int fegpu_batch_wait(fegpu_batch *b) {
 int fegpu_batch_run(fegpu_batch *b) {
   const int st = fegpu_batch_launch(b);
   return st != FEGPU_OK ? st : fegpu_batch_wait(b);
+}
+
+int fegpu_batch_withhold(fegpu_batch *b, int64_t job) {
+  return batch_guard([&] {
+    FEGPU_REQUIRE(b, "null handle");
+    FEGPU_REQUIRE(job >= -1 && job < static_cast<int64_t>(b->jobs.size()), "batch: no such job");
+    int ctr = -1;
+    if (job >= 0) {
+      // completion counters: two per chunk of every job, jobs in order
+      // (batch_queue.cpp); the job's first element stage is its first counter
+      ctr = 0;
+      for (int64_t j = 0; j < job; ++j)
+        ctr += 2 * std::max<int>(0, static_cast<int>(b->jobs[j].K->dm->chunk_nodes.size()) - 1);
+    }
+    b->withheld = ctr;
+    b->dirty = true;  // a captured kernel argument
+    drop_graph(b);
+  });
 }
 
 int fegpu_batch_set_wait_limit(fegpu_batch *b, double seconds) {

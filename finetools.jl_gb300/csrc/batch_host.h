@@ -80,9 +80,11 @@ size_t batch_smem_bytes(const std::vector<BatchJob> &jobs,
 // Persistent grid: resident CTAs per SM x SMs x share (0 < share <= 1).
 int batch_grid(int num_sms, size_t smem, int nitems, double share);
 
-// Launch of the persistent kernel (status: 0 ok, 1 a wait ran out of time).
+// Launch of the persistent kernel (status: 0 ok, 1 a wait ran out of time);
+// withheld >= 0 withholds the completions of that counter (the failure path's
+// test: the items waiting on it run out of time).
 void launch_batch_kernel(int grid, size_t smem, cudaStream_t s, const BatchJob *jobs,
                          const BatchItem *items, int nitems, int *next, int *counters,
-                         int *status, double wait_s);
+                         int *status, double wait_s, int withheld = -1);
 
 }  // namespace fegpu

@@ -337,7 +337,10 @@ __global__ void __launch_bounds__(kFormThreads) k_form(const KArgs a) {
     const int64_t eb = a.e0 + tile * te;
     const int ne = static_cast<int>(min(static_cast<int64_t>(te), a.e1 - eb));
     __syncthreads();
-    for (int i = tid; i < ne * NNE; i += nth) sConn[i] = a.conn[eb * NNE + i];
+    for (int i = tid; i < ne * NNE; i += nth) {
+      const int32_t c = a.conn[eb * NNE + i];
+      sConn[i] = dcheck(a.check, CK_CONN, c, a.nnodes) ? c : 0;  // debug builds
+    }
     __syncthreads();
     for (int i = tid; i < ne * NNE; i += nth) {
       const double *p = a.xyz + 4 * static_cast<int64_t>(sConn[i]);
@@ -445,7 +448,10 @@ __global__ void __launch_bounds__(kFormThreads) k_form(const KArgs a) {
         }
         const int32_t A = sConn[e * NNE + k];
 #pragma unroll
-        for (int c = 0; c < NDN; ++c) a.val[a.dof[A * NDN + c]] += fe[c];
+        for (int c = 0; c < NDN; ++c) {
+          const int32_t r = a.dof[A * NDN + c];
+          if (dcheck(a.check, CK_VECTOR, r, a.nnz)) a.val[r] += fe[c];  // debug builds
+        }
       }
       continue;
     }
@@ -590,6 +596,17 @@ __global__ void __launch_bounds__(kFormThreads) k_form(const KArgs a) {
         cB[ii] = !off_diag ? 0
                  : a.colperm ? a.colperm[a.cpoff[B] * NDN + NDN * pBA + ii]
                              : static_cast<int64_t>(NDN * pBA + ii);
+      }
+      if constexpr (kDeviceChecks) {  // debug builds: every slot inside the values
+        bool inside = true;
+#pragma unroll
+        for (int ii = 0; ii < NDN; ++ii)
+#pragma unroll
+          for (int jj = 0; jj < NDN; ++jj) {
+            inside = inside && dcheck(a.check, CK_SCATTER, rA[ii] + cA[jj], a.nnz);
+            if (off_diag) inside = inside && dcheck(a.check, CK_SCATTER, rB[jj] + cB[ii], a.nnz);
+          }
+        if (!inside) continue;
       }
       double cur[NDN][NDN], curt[NDN][NDN];
 #pragma unroll

@@ -103,7 +103,7 @@ __device__ __forceinline__ void gather_node_exact(const GArgs &g, int32_t A, dou
         // S + S': (S + S) / 2 on the diagonal
         v = (c == self * NDN + i) ? __dmul_rn(__dadd_rn(l, l), 0.5) : __dadd_rn(l, up[i * cmax + c]);
       }
-      g.val[base[i] + off] = v;
+      if (dcheck(g.check, CK_GATHER, base[i] + off, g.nnz)) g.val[base[i] + off] = v;
     }
   }
   __syncwarp();
@@ -262,6 +262,8 @@ void run_exact(fegpu_dofmap *dm, int form, KArgs &a, bool symmetric) {
   g.cpoff = dm->contiguous ? nullptr : dm->cpoff.as<int64_t>();
   g.val = a.val;
   g.maxdeg = dm->maxdeg;
+  g.check = a.check;
+  g.nnz = dm->nnz;
   const int64_t nch = static_cast<int64_t>(dm->x_chunk_nodes.size()) - 1;
   cudaStream_t s0 = ctx->stream;
   if (!ctx->side) FEGPU_CUDA(cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking));

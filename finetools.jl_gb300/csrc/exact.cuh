@@ -131,7 +131,10 @@ __global__ void __launch_bounds__(kExactThreads) k_blocks_exact(const KArgs a) {
     const int64_t eb = a.e0 + tile * te;
     const int ne = static_cast<int>(min(static_cast<int64_t>(te), a.e1 - eb));
     __syncthreads();
-    for (int i = tid; i < ne * NNE; i += nth) sConn[i] = a.conn[eb * NNE + i];
+    for (int i = tid; i < ne * NNE; i += nth) {
+      const int32_t c = a.conn[eb * NNE + i];
+      sConn[i] = dcheck(a.check, CK_CONN, c, a.nnodes) ? c : 0;  // debug builds
+    }
     __syncthreads();
     for (int i = tid; i < ne * NNE; i += nth) {
       const double *p = a.xyz + 4 * static_cast<int64_t>(sConn[i]);

@@ -82,6 +82,33 @@ inline int max_qp(int et) {
   return 0;
 }
 
+// ---- device index checks (debug builds, -DFEGPU_DEVICE_CHECKS) ---------------
+// The kernels check the node numbers they read and the CSR slots they write;
+// the first violation (site << 56 | index) goes to the context's check word,
+// the access is skipped, and the entry point returns FEGPU_ERR_DEVICE.  Off in
+// regular builds: the checks then compile to nothing.
+enum CheckSite { CK_CONN = 1, CK_SCATTER = 2, CK_GATHER = 3, CK_VECTOR = 4 };
+#if defined(FEGPU_DEVICE_CHECKS)
+constexpr bool kDeviceChecks = true;
+#else
+constexpr bool kDeviceChecks = false;
+#endif
+#if defined(__CUDACC__)
+// true when 0 <= i < n; otherwise records (site, i) as the first violation
+__device__ __forceinline__ bool dcheck(unsigned long long *word, int site, int64_t i, int64_t n) {
+  if constexpr (!kDeviceChecks) {
+    return true;
+  } else {
+    if (i >= 0 && i < n) return true;
+    if (word)
+      atomicCAS(word, 0ull,
+                (static_cast<unsigned long long>(site) << 56) |
+                    (static_cast<unsigned long long>(i) & ((1ull << 56) - 1ull)));
+    return false;
+  }
+}
+#endif
+
 }  // namespace fegpu
 
 // ---- handles (opaque to callers) -------------------------------------------
@@ -103,6 +130,8 @@ struct fegpu_context {
   cudaStream_t export_stream = nullptr;
   // status word of the tensor-core element kernel (0 = ok), made on first use
   fegpu::DevBuf tc_status;
+  // first device index-check violation (builds with device checks only)
+  fegpu::DevBuf check_word;
 };
 
 struct fegpu_femm {
@@ -219,6 +248,9 @@ struct KArgs {
   int *status;             // device status word (0 = ok)
   float *ke;               // block-output mode: element blocks of elements e0.. (or null)
   double *ke64;            // reference-order path: FP64 blocks of elements e0..
+  unsigned long long *check;  // device index checks: first violation (or null)
+  int64_t nnz;             // values behind val (CSR values, or the vector's length)
+  int64_t nnodes;          // node count (coordinates behind xyz)
 };
 
 // Launch one colour of one form.  Returns the number of kernel launches made.
@@ -254,6 +286,8 @@ struct GArgs {
   const int64_t *cpoff;
   double *val;
   int maxdeg;
+  unsigned long long *check;  // device index checks: first violation (or null)
+  int64_t nnz;
 };
 void build_gather_plan(fegpu_dofmap *dm, int nblk_values);
 // node -> element lists and element-order slot maps (once per dofmap); the
@@ -285,6 +319,9 @@ void pack_geometry(const double *src_colmajor, int64_t nnodes, int sdim, double 
 
 // ---- shared by the entry points -----------------------------------------------------
 KArgs base_args(fegpu_matrix *K, fegpu_dofmap *dm);
+// builds with device checks: reads (and clears) the context's check word and
+// throws FEGPU_ERR_DEVICE naming the first violation; otherwise nothing
+void device_checks(fegpu_context *ctx, cudaStream_t s);
 // work queued on s after this call may overwrite K's values: it first waits
 // (on the device) for a copy of them still in flight to the host
 void await_export(fegpu_matrix *K, cudaStream_t s);

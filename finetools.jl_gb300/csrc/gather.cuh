@@ -217,7 +217,9 @@ __device__ __forceinline__ void gather_node(const GArgs &g, int32_t A, float *ac
     float h[NDN], l[NDN];
     acc.get(c, h, l);
 #pragma unroll
-    for (int i = 0; i < NDN; ++i) g.val[base[i] + off] = ff_to_double(h[i], l[i]);
+    for (int i = 0; i < NDN; ++i)
+      if (dcheck(g.check, CK_GATHER, base[i] + off, g.nnz))  // debug builds
+        g.val[base[i] + off] = ff_to_double(h[i], l[i]);
   }
   __syncwarp();
 }

@@ -142,7 +142,10 @@ __device__ __forceinline__ void mixed_tile(const KArgs &a, int64_t eb, int ne,
   const float odim = static_cast<float>(a.otherdim);
   {
     __syncthreads();
-    for (int i = tid; i < ne * NNE; i += nth) sConn[i] = a.conn[eb * NNE + i];
+    for (int i = tid; i < ne * NNE; i += nth) {
+      const int32_t c = a.conn[eb * NNE + i];
+      sConn[i] = dcheck(a.check, CK_CONN, c, a.nnodes) ? c : 0;  // debug builds
+    }
     __syncthreads();
     // A. FP32 coordinates relative to the first node
     for (int i = tid; i < ne * NNE; i += nth) {

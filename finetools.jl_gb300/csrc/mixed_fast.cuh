@@ -122,7 +122,10 @@ __device__ __forceinline__ void fast_geometry(const KArgs &a, int64_t eb, int ne
   const float tol = static_cast<float>(a.distort_tol);
   const float odim = static_cast<float>(a.otherdim);
   __syncthreads();  // the previous tile is done with shared memory
-  for (int i = tid; i < ne * NNE; i += nth) sConn[i] = a.conn[eb * NNE + i];
+  for (int i = tid; i < ne * NNE; i += nth) {
+    const int32_t c = a.conn[eb * NNE + i];
+    sConn[i] = dcheck(a.check, CK_CONN, c, a.nnodes) ? c : 0;  // debug builds
+  }
   if constexpr (FORM == F_ELAST_ISO) {
     for (int e = tid; e < ne; e += nth) {
       if (a.coef_kind == FEGPU_COEF_ISO_LAME) {

@@ -217,6 +217,8 @@ extern "C" int fegpu_bilform_lin_elastic_noalloc(fegpu_matrix *K, const fegpu_co
     g.cpoff = dm->contiguous ? nullptr : dm->cpoff.as<int64_t>();
     g.val = K->val.as<double>();
     g.maxdeg = dm->maxdeg;
+    g.check = a.check;
+    g.nnz = dm->nnz;
     await_export(K, s);
     a.status = status_address(ctx->device);  // enables the tensor-core element blocks
     const int64_t nch = static_cast<int64_t>(dm->na_chunk_nodes.size()) - 1;

@@ -97,6 +97,15 @@ int fegpu_context_stream(fegpu_context *ctx, void **stream);
  * (ms) and the number of kernels the library launched, and resets them when
  * reset != 0. */
 int fegpu_context_timing(fegpu_context *ctx, int enable);
+/* Whether this build checks device indices (no reference counterpart: the
+ * reference's assemble! bounds-checks every DOF, src/AssemblyModule.jl:
+ * 519-524).  A library built with FEGPU_DEVICE_CHECKS (build.py
+ * --device-checks, libfegpu_checked.so) checks in its kernels the node
+ * numbers they read and the CSR slots and vector entries they write, skips an
+ * access out of range and records the first one; the entry point then
+ * returns FEGPU_ERR_DEVICE naming it.  Regular builds compile the checks
+ * away. */
+int fegpu_context_device_checks(fegpu_context *ctx, int *enabled);
 int fegpu_context_kernel_stats(fegpu_context *ctx, double *kernel_ms, int64_t *launches,
                                int reset);
 
@@ -280,6 +289,13 @@ int fegpu_batch_set_coef(fegpu_batch *b, int64_t job, const fegpu_coef *cf);
 int fegpu_batch_tune(fegpu_batch *b, const char *cache_path);
 int fegpu_batch_tile(fegpu_batch *b, int64_t job, int *elements_per_tile);
 int fegpu_batch_set_wait_limit(fegpu_batch *b, double seconds);
+/* Test of the failure path (no reference counterpart): job >= 0 withholds the
+ * completion count of that job's first element stage, a counter nothing else
+ * raises, so the items that depend on it wait until the wait limit, the
+ * kernel skips the rest and ends, and fegpu_batch_wait returns
+ * FEGPU_ERR_DEVICE; job = -1 restores normal runs.  No device fault is
+ * involved: every wait is bounded. */
+int fegpu_batch_withhold(fegpu_batch *b, int64_t job);
 /* launch (asynchronous, on the context stream) / wait and check / both */
 int fegpu_batch_launch(fegpu_batch *b);
 int fegpu_batch_wait(fegpu_batch *b);

@@ -211,3 +211,31 @@ def test_batch_rejects_unbatched_kinds(ft):
     with pytest.raises(ValueError):
         b.add("convection", femm, ft.NodalField(fens.xyz), _field(ft, fens.count(), 1),
               ft.DataCache(1.0))
+
+
+def test_dependency_wait_runs_out_and_the_next_run_recovers(ft):
+    """The failure path of the persistent kernel without a device fault: the
+    completion of a job's first element stage is withheld (a counter nothing
+    then raises), so the gather that depends on it waits until the wait limit
+    (0.05 s here), the kernel skips the rest and ends, and the run reports
+    FEGPU_ERR_DEVICE through the C ABI.  The same batch then runs cleanly at
+    the default limit and its matrices equal those of the run before."""
+    import time
+    from importlib import import_module
+    nat = import_module(ft.__name__ + "._native")
+    b = ft.AssemblyBatch()
+    mats = [b.add(*_case(ft, name)) for name in ("h20_elastic_per_element", "t10_elastic")]
+    b.run()
+    ref = [M.values() for M in mats]
+    b.set_wait_limit(0.05)
+    b.withhold(1)
+    t0 = time.perf_counter()
+    b.launch()
+    with pytest.raises(nat.FegpuError, match="waited past its time limit"):
+        b.wait()
+    assert time.perf_counter() - t0 < 10.0
+    b.withhold(-1)
+    b.set_wait_limit(5.0)
+    b.run()
+    for M, r in zip(mats, ref):
+        assert np.array_equal(M.values().view(np.int64), r.view(np.int64))
