@@ -898,26 +898,64 @@ def _percentiles(lat):
     return float(np.percentile(a, 50)), float(np.percentile(a, 99))
 
 
+def _serve_stream(srv, rng, rate, nreq, submit, live, elems, admit_at=None, admit=None):
+    """A Poisson stream of nreq requests at `rate` per second over the meshes
+    in `live` (a list it may grow: admit() is called once, after admit_at
+    requests, while the stream runs); returns the latencies (ms) and the
+    elements/s over the stream."""
+    arr = np.cumsum(rng.exponential(1.0 / rate, nreq))
+    t_start = time.perf_counter()
+    reqs, work = [], 0.0
+    for i, a in enumerate(arr):
+        if admit is not None and i == admit_at:
+            admit()
+        dt = t_start + a - time.perf_counter()
+        if dt > 0:
+            time.sleep(dt)
+        k = live[int(rng.integers(0, len(live)))]
+        reqs.append(submit(k, int(rng.integers(0, 2)), int(rng.integers(0, 2))))
+        work += elems[k]
+    lat = [srv.wait(r) for r in reqs]
+    return lat, work / (time.perf_counter() - t_start)
+
+
 def bench_serve(ft, torch, lib, stream, args, local, dist):
+    """32 resident meshes; rounds of bounded work; the last 8 meshes are
+    admitted while the first stream runs; Poisson streams at 0.3 - 1.1 of the
+    measured capacity; the FP64 comparison is a stream through an FP64 server."""
     import gc
     t0 = time.perf_counter()
     cases = serve_cases(ft, args.serve_meshes, device=local)
     mesh_s = time.perf_counter() - t0
     rng = np.random.default_rng(7)
     payloads = _request_payloads(cases, rng)
-    t0 = time.perf_counter()
-    srv = ft.AssemblyServer(lanes=args.serve_lanes, max_jobs=16, device=local)
-    ids = []
-    for c in cases:
+    srv = ft.AssemblyServer(lanes=args.serve_lanes, max_jobs=64, device=local)
+    ids = {}
+    refused = []
+
+    def admit(k):
+        """Admission by the library's memory estimate, then add_mesh (which
+        checks the memory serving the mesh still needs)."""
+        c = cases[k]
+        fe = c["femm"].integdomain.fes
+        need = ft.estimate_mesh_bytes(fe.code, c["elements"], c["nodes"],
+                                      1 if c["form"] == "diffusion" else 3)
         free, _ = srv.memory()
-        # admission: the pattern, values, slot maps and ring of the new mesh must fit
-        need = 40 * c["elements"] * (100 if c["type"] == "T10" else 8) * 3
-        if free < need:
-            break
-        ids.append(srv.add_mesh(c["form"], c["femm"], c["geom"], c["u"], c["cf"]))
-    cases = cases[:len(ids)]
+        if free - (1 << 30) < need:
+            refused.append(k)
+            return False
+        try:
+            ids[k] = srv.add_mesh(c["form"], c["femm"], c["geom"], c["u"], c["cf"])
+        except ft.FegpuError:
+            refused.append(k)
+            return False
+        return True
+
+    n_initial = max(1, (3 * len(cases)) // 4)
+    t0 = time.perf_counter()
+    for k in range(n_initial):
+        admit(k)
     setup_s = time.perf_counter() - t0
-    n = len(cases)
     elems = np.array([c["elements"] for c in cases], dtype=np.float64)
 
     def submit(k, kind, v):
@@ -926,95 +964,84 @@ def bench_serve(ft, torch, lib, stream, args, local, dist):
         return srv.submit_coef(mid, p["coef"][v]) if kind == 0 else \
             srv.submit_coords(mid, p["coords"][v])
 
-    # capacity: every mesh re-assembled, all requests present at once
-    for rep in range(2):
-        srv.hold(True)
-        reqs = [submit(k, 0, rep % 2) for k in range(n)]
-        t0 = time.perf_counter()
-        srv.hold(False)
-        for r in reqs:
-            srv.wait(r)
-        burst_s = time.perf_counter() - t0
-    capacity = elems.sum() / burst_s                  # elements/s
-    mean_service = elems.mean() / capacity            # s per request at saturation
-    res = {"meshes": n, "elements": int(elems.sum()),
-           "types": {t: sum(1 for c in cases if c["type"] == t) for t in ("H8", "T10")},
-           "lanes": args.serve_lanes, "setup_s": {"meshes": mesh_s, "register": setup_s},
-           "capacity_elements_per_s": capacity, "sweep": []}
+    def capacity():
+        live = sorted(ids)
+        for rep in range(2):
+            srv.hold(True)
+            reqs = [submit(k, 0, rep % 2) for k in live]
+            t0 = time.perf_counter()
+            srv.hold(False)
+            for r in reqs:
+                srv.wait(r)
+            burst_s = time.perf_counter() - t0
+        return elems[live].sum() / burst_s, elems[live].mean()
+
+    cap0, mean0 = capacity()
+    res = {"meshes_initial": len(ids), "lanes_rounds_in_flight": args.serve_lanes,
+           "slice_elements": 262144, "setup_s": {"meshes": mesh_s, "register": setup_s},
+           "capacity_elements_per_s_initial": cap0, "sweep": []}
     nreq = args.serve_requests
-    for frac in (0.3, 0.6, 0.9, 1.1):
-        rate = frac / mean_service                    # requests/s
-        arr = np.cumsum(rng.exponential(1.0 / rate, nreq))
-        which = rng.integers(0, n, nreq)
-        kinds = rng.integers(0, 2, nreq)
-        t_start = time.perf_counter()
-        reqs = []
-        for a, k, kd in zip(arr, which, kinds):
-            dt = t_start + a - time.perf_counter()
-            if dt > 0:
-                time.sleep(dt)
-            reqs.append(submit(int(k), int(kd), int(rng.integers(0, 2))))
-        lat = [srv.wait(r) for r in reqs]
-        span = time.perf_counter() - t_start
+    late = list(range(n_initial, len(cases)))
+    admitted_mid = []
+
+    def admit_late():
+        for k in late:
+            if admit(k):
+                admitted_mid.append(k)
+
+    for i, frac in enumerate((0.3, 0.6, 0.9, 1.1)):
+        cap, mean_e = (cap0, mean0) if i == 0 else capacity()
+        rate = frac * cap / mean_e
+        live = sorted(ids)
+        lat, eps = _serve_stream(srv, rng, rate, nreq, submit, live, elems,
+                                 admit_at=nreq // 2 if i == 0 else None,
+                                 admit=admit_late if i == 0 else None)
+        if i == 0:
+            res["capacity_elements_per_s"] = capacity()[0]  # all meshes admitted
         p50, p99 = _percentiles(lat)
         res["sweep"].append({"load": frac, "rate_per_s": rate, "requests": nreq,
-                             "p50_ms": p50, "p99_ms": p99, "p99_over_p50": p99 / p50,
-                             "elements_per_s": float(elems[which].sum() / span)})
+                             "meshes": len(live), "p50_ms": p50, "p99_ms": p99,
+                             "p99_over_p50": p99 / p50, "elements_per_s": float(eps)})
+    res["admitted_mid_stream"] = len(admitted_mid)
+    res["refused"] = len(refused)
+    res["meshes"] = len(ids)
+    res["elements"] = int(elems[sorted(ids)].sum())
+    res["types"] = {t: sum(1 for k in ids if cases[k]["type"] == t) for t in ("H8", "T10")}
     res["server"] = srv.stats()
+    res["held_bytes"] = srv.mesh_bytes()
     srv.close()
-    # FP64: the same kind of stream served one request at a time by single calls
-    asm = ft.SysmatAssemblerGPU(precision="fp64", result="device", device=local)
-    mats = [_single_call_serve(ft, c, asm) for c in cases]
-    torch.cuda.synchronize()
+    # FP64: the same kind of stream through an FP64 server (FEGPU_FP64_FAST:
+    # the single-call FP64 form, one request at a time, in the same loop)
+    fsrv = ft.AssemblyServer(lanes=1, device=local, precision="fp64_fast")
+    fids = {k: fsrv.add_mesh(cases[k]["form"], cases[k]["femm"], cases[k]["geom"], cases[k]["u"],
+                             cases[k]["cf"]) for k in sorted(ids)}
+
+    def fsubmit(k, kind, v):
+        mid = fids[k][0]
+        p = payloads[k]
+        return fsrv.submit_coef(mid, p["coef"][v]) if kind == 0 else \
+            fsrv.submit_coords(mid, p["coords"][v])
+
+    live = sorted(fids)
+    fsrv.hold(True)
+    reqs = [fsubmit(k, 0, 0) for k in live]
     t0 = time.perf_counter()
-    for k in range(n):
-        _fp64_request(ft, lib, cases[k], mats[k], payloads[k], 0, 0)
-    fp64_capacity = elems.sum() / (time.perf_counter() - t0)
-    rate = 0.6 * fp64_capacity / elems.mean()
-    nr = max(32, nreq // 2)
-    arr = np.cumsum(rng.exponential(1.0 / rate, nr))
-    which = rng.integers(0, n, nr)
-    kinds = rng.integers(0, 2, nr)
-    t_start = time.perf_counter()
-    lat = []
-    for a, k, kd in zip(arr, which, kinds):
-        dt = t_start + a - time.perf_counter()
-        if dt > 0:
-            time.sleep(dt)
-        _fp64_request(ft, lib, cases[int(k)], mats[int(k)], payloads[int(k)], int(kd), 1)
-        lat.append(1e3 * (time.perf_counter() - (t_start + a)))
+    fsrv.hold(False)
+    for r in reqs:
+        fsrv.wait(r)
+    fp64_capacity = elems[live].sum() / (time.perf_counter() - t0)
+    rate = 0.6 * fp64_capacity / elems[live].mean()
+    lat, eps = _serve_stream(fsrv, rng, rate, max(32, nreq // 2), fsubmit, live, elems)
     p50, p99 = _percentiles(lat)
-    res["fp64_one_request_at_a_time"] = {"capacity_elements_per_s": fp64_capacity,
-                                         "load": 0.6, "p50_ms": p50, "p99_ms": p99,
-                                         "p99_over_p50": p99 / p50}
-    res["capacity_mixed_over_fp64"] = capacity / fp64_capacity
-    del mats, asm, srv, ids, cases
+    res["fp64_fast_server"] = {"capacity_elements_per_s": fp64_capacity, "load": 0.6,
+                               "p50_ms": p50, "p99_ms": p99, "p99_over_p50": p99 / p50,
+                               "elements_per_s": float(eps)}
+    res["capacity_mixed_over_fp64_fast"] = res["capacity_elements_per_s"] / fp64_capacity
+    fsrv.close()
+    del fids, ids, cases, srv, fsrv
     gc.collect()
     torch.cuda.empty_cache()
     return res
-
-
-def _single_call_serve(ft, c, asm):
-    if c["form"] == "diffusion":
-        return ft.bilform_diffusion(c["femm"], asm, c["geom"], c["u"], c["cf"])
-    return ft.bilform_lin_elastic(c["femm"], asm, c["geom"], c["u"], ft.DeforModelRed3D, c["cf"])
-
-
-def _fp64_request(ft, lib, c, K, payload, kind, v):
-    """One FP64 re-assembly through the C ABI: new coordinates or coefficients."""
-    L, nat = lib.L, lib.nat
-    if kind == 1:
-        x = payload["coords"][v]
-        nat.check(L.fegpu_femm_set_geometry(c["femm"]._h, 3, x.ctypes.data))
-        data = c["cf"].values if c["form"] == "diffusion" else c["cf"].lame
-    else:
-        data = payload["coef"][v]
-    if c["form"] == "diffusion":
-        coef = nat.Coef(nat.COEF_PER_ELEMENT, 1, data.ctypes.data)
-        nat.check(L.fegpu_bilform_diffusion(K.h, C.byref(coef), nat.FP64))
-    else:
-        coef = nat.Coef(nat.COEF_ISO_LAME, 2, data.ctypes.data)
-        nat.check(L.fegpu_bilform_lin_elastic(K.h, C.byref(coef), nat.FP64))
 
 
 def bench_h8(ft, torch, lib, stream, args, local, dist):

@@ -10,7 +10,7 @@ package is the host-side mirror of the reference's Julia interface.
 """
 from ._native import FegpuError, load as load_library
 from .batch import AssemblyBatch
-from .serve import AssemblyServer
+from .serve import AssemblyServer, estimate_mesh_bytes
 from .assembly import (DeviceMatrix, SysmatAssemblerGPU, SysmatAssemblerSparseDiagGPU,
                        SysmatAssemblerFFBlockGPU, SysmatAssemblerSparseHRZLumpingSymmGPU,
                        SysvecAssemblerFBlockGPU, SysvecAssemblerGPU, assemble,

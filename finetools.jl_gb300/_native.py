@@ -38,7 +38,10 @@ EXPORTS = [
     "fegpu_batch_create", "fegpu_batch_destroy", "fegpu_batch_add", "fegpu_batch_set_coef",
     "fegpu_batch_tune", "fegpu_batch_tile", "fegpu_batch_set_wait_limit", "fegpu_batch_withhold", "fegpu_batch_launch",
     "fegpu_batch_wait", "fegpu_batch_run", "fegpu_batch_stats",
-    "fegpu_server_create", "fegpu_server_destroy", "fegpu_server_add_mesh", "fegpu_server_submit",
+    "fegpu_server_create", "fegpu_server_destroy", "fegpu_server_set_precision",
+    "fegpu_server_set_slice", "fegpu_server_set_memory_limit", "fegpu_server_add_mesh",
+    "fegpu_server_remove_mesh", "fegpu_server_mesh_bytes", "fegpu_estimate_mesh_bytes",
+    "fegpu_server_submit", "fegpu_server_cancel",
     "fegpu_server_wait", "fegpu_server_drain", "fegpu_server_hold", "fegpu_server_stats",
     "fegpu_server_memory",
 ]
@@ -123,6 +126,13 @@ def load(path: str = LIBPATH):
         "fegpu_batch_stats": ([vp, p64, p64], i32),
         "fegpu_server_create": ([vp, i32, i32, pp], i32),
         "fegpu_server_destroy": ([vp], i32),
+        "fegpu_server_set_precision": ([vp, i32], i32),
+        "fegpu_server_set_slice": ([vp, i64], i32),
+        "fegpu_server_set_memory_limit": ([vp, i64], i32),
+        "fegpu_server_remove_mesh": ([vp, i64], i32),
+        "fegpu_server_mesh_bytes": ([vp, i64, p64], i32),
+        "fegpu_estimate_mesh_bytes": ([i32, i64, i64, i32, p64], i32),
+        "fegpu_server_cancel": ([vp, i64], i32),
         "fegpu_server_add_mesh": ([vp, vp, i32, C.POINTER(Coef), i32, p64], i32),
         "fegpu_server_submit": ([vp, i64, i32, vp, i64, p64], i32),
         "fegpu_server_wait": ([vp, i64, C.POINTER(C.c_double)], i32),

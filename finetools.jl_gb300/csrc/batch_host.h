@@ -69,9 +69,15 @@ void make_batch_job(fegpu_matrix *K, int form, int code, int m, const fegpu_coef
 // previous chunk's gather.  Jobs
 // pass through a window (one stage of each per round) holding the jobs whose
 // live ring chunks fit in `live_budget` bytes (at least two jobs).
+// ranges (optional): per job the chunks [c0, c1) to run (a slice of the job,
+// whose earlier chunks ran in launches before this one on the same stream).
+struct ChunkRange {
+  int64_t c0, c1;
+};
 int build_batch_items(const std::vector<BatchJob> &jobs,
                       const std::vector<const fegpu_dofmap *> &dms, size_t live_budget,
-                      std::vector<BatchItem> &items);
+                      std::vector<BatchItem> &items,
+                      const std::vector<ChunkRange> *ranges = nullptr);
 
 // Dynamic shared memory the kernel needs for these jobs.
 size_t batch_smem_bytes(const std::vector<BatchJob> &jobs,

@@ -8,33 +8,49 @@ namespace fegpu {
 
 int build_batch_items(const std::vector<BatchJob> &jobs,
                       const std::vector<const fegpu_dofmap *> &dms, size_t live_budget,
-                      std::vector<BatchItem> &items) {
+                      std::vector<BatchItem> &items, const std::vector<ChunkRange> *ranges) {
   const size_t njobs = jobs.size();
   items.clear();
   std::vector<int> base(njobs), nchunk(njobs);
+  std::vector<int64_t> first(njobs, 0);
   int ncount = 0;
   for (size_t j = 0; j < njobs; ++j) {
-    nchunk[j] = static_cast<int>(dms[j]->chunk_nodes.size()) - 1;
+    const int64_t all = static_cast<int64_t>(dms[j]->chunk_nodes.size()) - 1;
+    if (ranges) {
+      const ChunkRange r = (*ranges)[j];
+      FEGPU_REQUIRE(0 <= r.c0 && r.c0 <= r.c1 && r.c1 <= std::max<int64_t>(all, 0),
+                    "batch: chunk range outside the job");
+      first[j] = r.c0;
+      nchunk[j] = static_cast<int>(r.c1 - r.c0);
+    } else {
+      nchunk[j] = static_cast<int>(all);
+    }
     base[j] = ncount;
     ncount += 2 * std::max(nchunk[j], 0);
   }
   std::vector<int> count(std::max(ncount, 1), 0);  // items per stage
-  // counters: E(c) -> base + 2c, G(c) -> base + 2c + 1
+  // counters: E(c) -> base + 2(c - first), G(c) -> base + 2(c - first) + 1.
+  // A dependency on a stage before the job's first chunk (a slice continuing a
+  // job run by an earlier launch on the same stream) is already met and is
+  // left out.
   auto emit_stage = [&](size_t j, bool gather, int64_t c) {
     const BatchJob &J = jobs[j];
     const fegpu_dofmap *dm = dms[j];
-    const int ctr = base[j] + 2 * static_cast<int>(c) + (gather ? 1 : 0);
+    const int64_t c0 = first[j];
+    auto ctr_of = [&](int64_t cc, bool g) { return base[j] + 2 * static_cast<int>(cc - c0) + (g ? 1 : 0); };
+    const int ctr = ctr_of(c, gather);
     int dep[2] = {-1, -1}, target[2] = {0, 0};
     if (!gather) {
-      if (c >= 1) dep[0] = base[j] + 2 * static_cast<int>(c - 1);
+      if (c - 1 >= c0) dep[0] = ctr_of(c - 1, false);
       // the ring slot of chunk c last held chunk c - ring, read by gathers up
       // to G(c - ring + span)
-      if (c >= dm->ring) dep[1] = base[j] + 2 * static_cast<int>(c - dm->ring + dm->span) + 1;
+      if (c >= dm->ring && c - dm->ring + dm->span >= c0)
+        dep[1] = ctr_of(c - dm->ring + dm->span, true);
     } else {
       // G(c) reads the blocks of chunks c - span .. c; gathers complete in
       // order, so the wait of E(c + ring) above covers every reader of a slot
-      dep[0] = base[j] + 2 * static_cast<int>(c);
-      if (c >= 1) dep[1] = base[j] + 2 * static_cast<int>(c - 1) + 1;
+      dep[0] = ctr_of(c, false);
+      if (c - 1 >= c0) dep[1] = ctr_of(c - 1, true);
     }
     for (int d = 0; d < 2; ++d)
       if (dep[d] >= 0) target[d] = count[dep[d]];
@@ -94,7 +110,7 @@ int build_batch_items(const std::vector<BatchJob> &jobs,
       bool gather;
       int64_t c;
       stage_of(j, next[j]++, gather, c);
-      emit_stage(j, gather, c);
+      emit_stage(j, gather, first[j] + c);
       if (next[j] < 2 * nchunk[j]) keep.push_back(j);
       else live -= live_bytes(j);
     }

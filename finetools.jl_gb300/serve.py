@@ -1,5 +1,5 @@
 """Serving loop: re-assembly requests on resident meshes (fegpu_server_* of
-include/fegpu.h), continuously batched onto the GPU.
+include/fegpu.h), continuously batched onto the GPU in rounds of bounded work.
 
     server = AssemblyServer(lanes=2)
     mid, K = server.add_mesh("lin_elastic", femm, geom, u, IsotropicElementwise(E, nu))
@@ -7,8 +7,11 @@ include/fegpu.h), continuously batched onto the GPU.
     rid2 = server.submit_coords(mid, new_xyz)         # (nnodes, 3)
     latency_ms = server.wait(rid)                     # K holds the request's matrix
 
-Each request is evaluated as the mixed-precision batch path; a request's
-matrix does not depend on which other requests shared its launch.
+Each request is evaluated as the mixed-precision batch path (or, with
+precision="fp64" / "fp64_fast", by the single-call FP64 form, one request at a
+time); a request's matrix does not depend on which other requests shared its
+rounds.  ``lanes`` is the number of rounds in flight.  A mesh is admitted only
+if the device memory it needs fits (and stays within memory_limit, if set).
 """
 from __future__ import annotations
 
@@ -33,15 +36,46 @@ def _destroy(L, h):
 class AssemblyServer:
     """Resident meshes + a worker thread that batches re-assembly requests."""
 
-    def __init__(self, lanes: int = 2, max_jobs: int = 64, device: int = 0):
+    def __init__(self, lanes: int = 2, max_jobs: int = 64, device: int = 0,
+                 precision: str = "mixed", slice_elements: int | None = None,
+                 memory_limit: int | None = None):
         L = nat.load()
         out = C.c_void_p()
         nat.check(L.fegpu_server_create(nat.context(device), int(lanes), int(max_jobs),
                                         C.byref(out)))
         self.h = out.value
         self.device = device
-        self.meshes = []        # (femm, geom, u, matrix) per mesh id
+        self.meshes = {}        # mesh id -> (femm, geom, u, matrix)
         self._fin = weakref.finalize(self, _destroy, L, self.h)
+        codes = {"mixed": nat.MIXED, "fp64": nat.FP64, "fp64_fast": nat.FP64_FAST}
+        if precision not in codes:
+            raise ValueError("precision must be 'mixed', 'fp64' or 'fp64_fast'")
+        if precision != "mixed":
+            nat.check(L.fegpu_server_set_precision(self.h, codes[precision]))
+        if slice_elements is not None:
+            nat.check(L.fegpu_server_set_slice(self.h, int(slice_elements)))
+        if memory_limit is not None:
+            self.set_memory_limit(memory_limit)
+
+    def set_memory_limit(self, nbytes: int):
+        """Refuse meshes that would bring the served meshes' device memory
+        above nbytes (0: no limit)."""
+        nat.check(nat.load().fegpu_server_set_memory_limit(self.h, int(nbytes)))
+
+    def mesh_bytes(self, mesh: int = -1) -> int:
+        """Device bytes held by a served mesh (-1: by all of them)."""
+        b = C.c_int64()
+        nat.check(nat.load().fegpu_server_mesh_bytes(self.h, int(mesh), C.byref(b)))
+        return b.value
+
+    def remove_mesh(self, mesh: int):
+        """Stop serving a mesh (no request of it waiting or in flight)."""
+        nat.check(nat.load().fegpu_server_remove_mesh(self.h, int(mesh)))
+        self.meshes.pop(mesh, None)
+
+    def cancel(self, request: int):
+        """Withdraw a request that is still waiting; its wait then raises."""
+        nat.check(nat.load().fegpu_server_cancel(self.h, int(request)))
 
     def close(self):
         """Stop the worker and free the server (its meshes' matrices stay)."""
@@ -65,7 +99,7 @@ class AssemblyServer:
         nat.check(L.fegpu_server_add_mesh(self.h, out.value, _FORMS[form], C.byref(coef), int(m),
                                           C.byref(mid)))
         M = DeviceMatrix(out.value, dm, drop_zeros=True)
-        self.meshes.append((femm, geom, u, M))
+        self.meshes[mid.value] = (femm, geom, u, M)
         return mid.value, M
 
     def submit_coef(self, mesh: int, values) -> int:
@@ -107,3 +141,13 @@ class AssemblyServer:
         f, t = C.c_int64(), C.c_int64()
         nat.check(nat.load().fegpu_server_memory(self.h, C.byref(f), C.byref(t)))
         return f.value, t.value
+
+
+def estimate_mesh_bytes(etype: int, nelem: int, nnodes: int, ndn: int) -> int:
+    """Device bytes a mesh of this size needs to be created and served (an
+    estimate from the element type's average node degree), for admission
+    before anything is allocated."""
+    b = C.c_int64()
+    nat.check(nat.load().fegpu_estimate_mesh_bytes(int(etype), int(nelem), int(nnodes), int(ndn),
+                                                   C.byref(b)))
+    return b.value

@@ -309,35 +309,67 @@ int fegpu_batch_stats(fegpu_batch *b, int64_t *jobs, int64_t *items);
  * -- and accepts requests that carry new per-element coefficients
  * (FEGPU_REQUEST_COEF: the same layout as the coefficient the mesh was added
  * with) or new node coordinates (FEGPU_REQUEST_COORDS: nnodes x sdim,
- * column-major, as geom.values).  A worker thread batches pending requests
- * (the oldest of every mesh not already on the GPU, up to max_jobs) into
- * launches of the persistent kernel on `lanes` streams, each lane using
- * 1/lanes of the GPU, so batches formed while others run overlap them.
- * Requests of one mesh complete in submission order; a request's result is
- * the mesh's matrix (values on the device, read with fegpu_matrix_copy_values
- * before the mesh's next request completes).  Every request is evaluated as
- * the batch path (FEGPU_MIXED); results do not depend on what else is in the
- * batch.  Latency = completion (host callback behind the kernel) - submit.
- * The data passed to fegpu_server_submit is copied; the matrices must outlive
- * the server; a coordinates request also changes the femm's geometry. */
+ * column-major, as geom.values).  A worker thread runs them in rounds: one
+ * launch of the persistent kernel over the whole GPU holds the next slice of
+ * every request in flight (at most slice_elements of its mesh's elements,
+ * fegpu_server_set_slice, default 262144) and the oldest waiting request of
+ * every mesh with none in flight, up to max_jobs; `lanes` rounds may be in
+ * flight (the next queued while one runs).  A request that arrives during a
+ * large assembly therefore waits at most a round, and a large request alone
+ * has the whole GPU.  Requests of one mesh complete in submission order; a
+ * request's result is the mesh's matrix (values on the device, read with
+ * fegpu_matrix_copy_values before the mesh's next request completes).  Every
+ * request is evaluated as the batch path (FEGPU_MIXED) and its matrix does
+ * not depend on what else shared its rounds.  Latency = completion (host
+ * callback behind the kernel) - submit.  The data passed to
+ * fegpu_server_submit is copied; the matrices must outlive the server; a
+ * coordinates request also changes the femm's geometry. */
 #define FEGPU_REQUEST_COEF 0
 #define FEGPU_REQUEST_COORDS 1
 typedef struct fegpu_server fegpu_server;
 int fegpu_server_create(fegpu_context *ctx, int lanes, int max_jobs, fegpu_server **out);
 int fegpu_server_destroy(fegpu_server *s);
+/* FEGPU_MIXED (default) or, before the first mesh is added, FEGPU_FP64 /
+ * FEGPU_FP64_FAST: the worker then runs each request by itself through the
+ * single-call form on the context's stream, in arrival order (the caller does
+ * not use that context meanwhile). */
+int fegpu_server_set_precision(fegpu_server *s, int precision);
+int fegpu_server_set_slice(fegpu_server *s, int64_t elements);
+/* Admission: fegpu_server_add_mesh returns FEGPU_ERR_MEMORY when the device
+ * memory the mesh still needs to be served (gather plan, block ring,
+ * coefficient and staging buffers) exceeds the free memory less a 256 MB
+ * reserve, or when a limit is set (bytes > 0) and the meshes' total device
+ * memory (their femm, pattern and values included) would exceed it; meshes
+ * can be added and removed while requests stream. */
+int fegpu_server_set_memory_limit(fegpu_server *s, int64_t bytes);
 int fegpu_server_add_mesh(fegpu_server *s, fegpu_matrix *K, int form, const fegpu_coef *cf,
                           int m, int64_t *mesh_id);
+/* stops serving a mesh (none of its requests waiting or in flight, else
+ * FEGPU_ERR_STATE) and frees what serving it added; the caller then destroys
+ * its matrix, dofmap and femm. */
+int fegpu_server_remove_mesh(fegpu_server *s, int64_t mesh_id);
+/* device bytes a served mesh holds (mesh_id < 0: all of them) */
+int fegpu_server_mesh_bytes(fegpu_server *s, int64_t mesh_id, int64_t *bytes);
+/* device bytes a mesh of this size needs to be created and served (femm,
+ * pattern, values, serving structures), from the average node degree of the
+ * element type: an estimate for admission before anything is allocated */
+int fegpu_estimate_mesh_bytes(int etype, int64_t nelem, int64_t nnodes, int ndn,
+                              int64_t *bytes);
 int fegpu_server_submit(fegpu_server *s, int64_t mesh_id, int kind, const double *data,
                         int64_t count, int64_t *request_id);
+/* a request still waiting is withdrawn (its wait returns FEGPU_ERR_STATE);
+ * one already running or done: FEGPU_ERR_STATE */
+int fegpu_server_cancel(fegpu_server *s, int64_t request_id);
 /* blocks until the request completed; its latency in ms; collects it */
 int fegpu_server_wait(fegpu_server *s, int64_t request_id, double *latency_ms);
-/* blocks until no request is pending or running */
+/* blocks until no request is waiting or in flight */
 int fegpu_server_drain(fegpu_server *s);
 /* hold = 1: no new launches (requests accumulate, e.g. during maintenance or
  * to admit a burst at once); hold = 0: resume */
 int fegpu_server_hold(fegpu_server *s, int hold);
+/* rounds launched, request slices run, requests waiting */
 int fegpu_server_stats(fegpu_server *s, int64_t *batches, int64_t *jobs, int64_t *pending);
-/* free and total device memory (admission of new meshes) */
+/* free and total device memory */
 int fegpu_server_memory(fegpu_server *s, int64_t *free_bytes, int64_t *total_bytes);
 
 /* ---- generic assembler for element matrices formed on the host -----------

@@ -139,3 +139,147 @@ def test_server_rejects_bad_requests(ft):
     free, total = srv.memory()
     assert 0 < free <= total
     srv.close()
+
+
+def test_large_request_in_slices_equals_single_call(ft):
+    """A request cut into several rounds (a few element chunks per round, its
+    block ring carried from one round to the next) gives the single-call
+    matrix bit for bit, also with other requests sharing its rounds."""
+    cases = _meshes(ft)
+    big = dict(cases[1])
+    fens, fes = ft.nearest_block("T10", 60000, seed=77)
+    femm = ft.FEMMBase(ft.IntegDomain(fes, ft.TetRule(4)))
+    rng = np.random.default_rng(12)
+    E = fes.count()
+    big.update(femm=femm, geom=ft.NodalField(fens.xyz), u=_field(ft, fens.count(), 3), E=E,
+               cf=ft.IsotropicElementwise(rng.lognormal(np.log(70e9), 1.0, E), np.full(E, 0.3)))
+    srv = ft.AssemblyServer(lanes=2, max_jobs=8, slice_elements=1)  # one chunk per round
+    mid, M = srv.add_mesh(big["form"], big["femm"], big["geom"], big["u"], big["cf"])
+    small = [srv.add_mesh(c["form"], c["femm"], c["geom"], c["u"], c["cf"]) for c in cases[2:4]]
+    cf, data = _new_coef(ft, big, rng)
+    scf = [_new_coef(ft, c, rng) for c in cases[2:4]]
+    srv.hold(True)
+    r = srv.submit_coef(mid, data)
+    rs = [srv.submit_coef(sm, d) for (sm, _), (_, d) in zip(small, scf)]
+    srv.hold(False)
+    srv.wait(r)
+    for x in rs:
+        srv.wait(x)
+    st = srv.stats()
+    nchunks = st["jobs"] - len(rs)
+    got = M.values()
+    got_small = [Ms.values() for _, Ms in small]
+    srv.close()
+    assert nchunks > 2 and st["batches"] >= nchunks  # the big request took several rounds
+    assert np.array_equal(got, _single_mixed(ft, big, cf))
+    for v, c, (cfs, _) in zip(got_small, cases[2:4], scf):
+        assert np.array_equal(v, _single_mixed(ft, c, cfs))
+
+
+def test_mesh_admitted_while_requests_stream(ft):
+    """A mesh is added while requests on the others are in flight; its own
+    requests then run in the same rounds, and every result equals the single
+    call."""
+    cases = _meshes(ft)
+    srv = ft.AssemblyServer(lanes=2, max_jobs=8, slice_elements=2000)
+    ids = [srv.add_mesh(c["form"], c["femm"], c["geom"], c["u"], c["cf"]) for c in cases[:3]]
+    rng = np.random.default_rng(4)
+    reqs = []
+    for _ in range(3):
+        for (mid, _), c in zip(ids, cases[:3]):
+            cf, data = _new_coef(ft, c, rng)
+            reqs.append((srv.submit_coef(mid, data), c, cf, mid))
+    late = cases[3]
+    lid, LM = srv.add_mesh(late["form"], late["femm"], late["geom"], late["u"], late["cf"])
+    lcf, ldata = _new_coef(ft, late, rng)
+    lreq = srv.submit_coef(lid, ldata)
+    last = {}
+    for rid, c, cf, mid in reqs:
+        srv.wait(rid)
+        last[mid] = (c, cf)
+    srv.wait(lreq)
+    got = {mid: M.values() for mid, M in ids}
+    lgot = LM.values()
+    srv.close()
+    for mid, (c, cf) in last.items():
+        assert np.array_equal(got[mid], _single_mixed(ft, c, cf))
+    assert np.array_equal(lgot, _single_mixed(ft, late, lcf))
+
+
+def test_admission_refused_above_the_memory_limit(ft):
+    """Out-of-memory on admission without exhausting the GPU: under a memory
+    limit the second mesh does not fit, add_mesh returns FEGPU_ERR_MEMORY
+    through the C ABI, and after the first mesh is removed it is admitted."""
+    cases = _meshes(ft)
+    srv = ft.AssemblyServer()
+    a, _ = srv.add_mesh(cases[0]["form"], cases[0]["femm"], cases[0]["geom"], cases[0]["u"],
+                        cases[0]["cf"])
+    held = srv.mesh_bytes(a)
+    assert held > 0 and srv.mesh_bytes() == held
+    srv.set_memory_limit(held + held // 4)
+    c = cases[1]
+    with pytest.raises(ft.FegpuError, match="not enough device memory"):
+        srv.add_mesh(c["form"], c["femm"], c["geom"], c["u"], c["cf"])
+    srv.remove_mesh(a)
+    assert srv.mesh_bytes() == 0
+    b, M = srv.add_mesh(c["form"], c["femm"], c["geom"], c["u"], c["cf"])
+    rng = np.random.default_rng(3)
+    cf, data = _new_coef(ft, c, rng)
+    srv.wait(srv.submit_coef(b, data))
+    got = M.values()
+    with pytest.raises(ft.FegpuError, match="no such mesh"):
+        srv.submit_coef(a, np.ones(cases[0]["E"]))
+    srv.close()
+    assert np.array_equal(got, _single_mixed(ft, c, cf))
+    # the estimate for admission before creating a mesh covers what it holds
+    fe = c["femm"].integdomain.fes
+    est = ft.estimate_mesh_bytes(fe.code, fe.count(), c["geom"].values.shape[0], 3)
+    assert est >= held // 2
+
+
+def test_cancelled_request(ft):
+    """A request still waiting is withdrawn: its wait returns an error status
+    through the C ABI; a running or finished one cannot be cancelled."""
+    c = _meshes(ft)[0]
+    srv = ft.AssemblyServer()
+    mid, M = srv.add_mesh(c["form"], c["femm"], c["geom"], c["u"], c["cf"])
+    rng = np.random.default_rng(8)
+    cf1, d1 = _new_coef(ft, c, rng)
+    cf2, d2 = _new_coef(ft, c, rng)
+    srv.hold(True)
+    r1 = srv.submit_coef(mid, d1)
+    r2 = srv.submit_coef(mid, d2)
+    srv.cancel(r2)
+    srv.hold(False)
+    srv.wait(r1)
+    with pytest.raises(ft.FegpuError, match="cancelled"):
+        srv.wait(r2)
+    with pytest.raises(ft.FegpuError, match="no such request"):
+        srv.cancel(r1)
+    got = M.values()
+    srv.close()
+    assert np.array_equal(got, _single_mixed(ft, c, cf1))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp64_fast"])
+def test_fp64_server(ft, precision):
+    """An FP64 server runs each request through the single-call FP64 form, one
+    at a time: results equal the single calls bit for bit."""
+    cases = _meshes(ft)[:2]
+    srv = ft.AssemblyServer(precision=precision)
+    ids = [srv.add_mesh(c["form"], c["femm"], c["geom"], c["u"], c["cf"]) for c in cases]
+    rng = np.random.default_rng(6)
+    out = []
+    for (mid, M), c in zip(ids, cases):
+        cf, data = _new_coef(ft, c, rng)
+        srv.wait(srv.submit_coef(mid, data))
+        out.append((M.values(), c, cf))
+    srv.close()
+    for v, c, cf in out:
+        asm = ft.SysmatAssemblerGPU(precision=precision, result="device")
+        if c["form"] == "diffusion":
+            ref = ft.bilform_diffusion(c["femm"], asm, c["geom"], c["u"], cf).values()
+        else:
+            ref = ft.bilform_lin_elastic(c["femm"], asm, c["geom"], c["u"], ft.DeforModelRed3D,
+                                         cf).values()
+        assert np.array_equal(v, ref)
