@@ -208,16 +208,15 @@ def test_mesh_admitted_while_requests_stream(ft):
 
 def test_admission_refused_above_the_memory_limit(ft):
     """Out-of-memory on admission without exhausting the GPU: under a memory
-    limit the second mesh does not fit, add_mesh returns FEGPU_ERR_MEMORY
-    through the C ABI, and after the first mesh is removed it is admitted."""
-    cases = _meshes(ft)
+    limit of 1.5 times one mesh's footprint, a second matrix of the same mesh
+    does not fit and add_mesh returns FEGPU_ERR_MEMORY through the C ABI;
+    after the first is removed the second is admitted and served."""
+    c = _meshes(ft)[0]
     srv = ft.AssemblyServer()
-    a, _ = srv.add_mesh(cases[0]["form"], cases[0]["femm"], cases[0]["geom"], cases[0]["u"],
-                        cases[0]["cf"])
+    a, _ = srv.add_mesh(c["form"], c["femm"], c["geom"], c["u"], c["cf"])
     held = srv.mesh_bytes(a)
     assert held > 0 and srv.mesh_bytes() == held
-    srv.set_memory_limit(held + held // 4)
-    c = cases[1]
+    srv.set_memory_limit(held + held // 2)
     with pytest.raises(ft.FegpuError, match="not enough device memory"):
         srv.add_mesh(c["form"], c["femm"], c["geom"], c["u"], c["cf"])
     srv.remove_mesh(a)
@@ -228,13 +227,13 @@ def test_admission_refused_above_the_memory_limit(ft):
     srv.wait(srv.submit_coef(b, data))
     got = M.values()
     with pytest.raises(ft.FegpuError, match="no such mesh"):
-        srv.submit_coef(a, np.ones(cases[0]["E"]))
+        srv.submit_coef(a, np.ones(c["E"]))
     srv.close()
     assert np.array_equal(got, _single_mixed(ft, c, cf))
-    # the estimate for admission before creating a mesh covers what it holds
+    # the estimate for admission before creating a mesh is of the same order
     fe = c["femm"].integdomain.fes
-    est = ft.estimate_mesh_bytes(fe.code, fe.count(), c["geom"].values.shape[0], 3)
-    assert est >= held // 2
+    est = ft.estimate_mesh_bytes(fe.code, fe.count(), c["geom"].values.shape[0], 1)
+    assert held // 4 <= est <= 8 * held
 
 
 def test_cancelled_request(ft):
