@@ -900,28 +900,60 @@ def _percentiles(lat):
 
 def _serve_stream(srv, rng, rate, nreq, submit, live, elems, admit_at=None, admit=None):
     """A Poisson stream of nreq requests at `rate` per second over the meshes
-    in `live` (a list it may grow: admit() is called once, after admit_at
-    requests, while the stream runs); returns the latencies (ms) and the
-    elements/s over the stream."""
+    in `live`; after admit_at requests admit() starts on a thread of its own
+    (a second client adding meshes while this one submits: it appends each
+    admitted mesh to `live`); returns the latencies (ms), the mesh of each
+    request and the elements/s over the stream."""
+    import threading
     arr = np.cumsum(rng.exponential(1.0 / rate, nreq))
     t_start = time.perf_counter()
-    reqs, work = [], 0.0
+    reqs, keys, work, th = [], [], 0.0, None
     for i, a in enumerate(arr):
         if admit is not None and i == admit_at:
-            admit()
+            th = threading.Thread(target=admit)
+            th.start()
         dt = t_start + a - time.perf_counter()
         if dt > 0:
             time.sleep(dt)
         k = live[int(rng.integers(0, len(live)))]
         reqs.append(submit(k, int(rng.integers(0, 2)), int(rng.integers(0, 2))))
+        keys.append(k)
         work += elems[k]
     lat = [srv.wait(r) for r in reqs]
-    return lat, work / (time.perf_counter() - t_start)
+    eps = work / (time.perf_counter() - t_start)
+    if th is not None:
+        th.join()
+    return lat, keys, eps
+
+
+def _latency_stats(lat, keys, alone):
+    """p50/p99 of the latencies, and of the slowdowns (latency over the
+    request's mesh served alone on an idle server); `floor` is the p99/p50
+    the same requests would show with no queueing at all (their alone
+    latencies), which bounds p99/p50 of the raw latencies from below when
+    request sizes differ by orders of magnitude."""
+    p50, p99 = _percentiles(lat)
+    sd = [x / alone[k] for x, k in zip(lat, keys)]
+    s50, s99 = _percentiles(sd)
+    f50, f99 = _percentiles([alone[k] for k in keys])
+    by_size = {}
+    for name, lo, hi in (("alone_lt_1ms", 0.0, 1.0), ("alone_1_to_5ms", 1.0, 5.0),
+                         ("alone_ge_5ms", 5.0, np.inf)):
+        sel = [x for x, k in zip(lat, keys) if lo <= alone[k] < hi]
+        if sel:
+            c50, c99 = _percentiles(sel)
+            by_size[name] = {"requests": len(sel), "p50_ms": c50, "p99_ms": c99,
+                             "p99_over_p50": c99 / c50}
+    return {"p50_ms": p50, "p99_ms": p99, "p99_over_p50": p99 / p50,
+            "floor_p99_over_p50": f99 / f50,
+            "slowdown_p50": s50, "slowdown_p99": s99, "slowdown_p99_over_p50": s99 / s50,
+            "by_size": by_size}
 
 
 def bench_serve(ft, torch, lib, stream, args, local, dist):
-    """32 resident meshes; rounds of bounded work; the last 8 meshes are
-    admitted while the first stream runs; Poisson streams at 0.3 - 1.1 of the
+    """32 resident meshes served on concurrent lanes in slices of bounded
+    work; the last 8 meshes are admitted (by a second client thread) while the
+    first stream runs; Poisson streams at 0.3 - 1.1 of the
     measured capacity; the FP64 comparison is a stream through an FP64 server."""
     import gc
     t0 = time.perf_counter()
@@ -929,7 +961,8 @@ def bench_serve(ft, torch, lib, stream, args, local, dist):
     mesh_s = time.perf_counter() - t0
     rng = np.random.default_rng(7)
     payloads = _request_payloads(cases, rng)
-    srv = ft.AssemblyServer(lanes=args.serve_lanes, max_jobs=64, device=local)
+    srv = ft.AssemblyServer(lanes=args.serve_lanes, max_jobs=64, device=local,
+                            slice_elements=args.serve_slice)
     ids = {}
     refused = []
 
@@ -977,8 +1010,8 @@ def bench_serve(ft, torch, lib, stream, args, local, dist):
         return elems[live].sum() / burst_s, elems[live].mean()
 
     cap0, mean0 = capacity()
-    res = {"meshes_initial": len(ids), "lanes_rounds_in_flight": args.serve_lanes,
-           "slice_elements": 262144, "setup_s": {"meshes": mesh_s, "register": setup_s},
+    res = {"meshes_initial": len(ids), "lanes": args.serve_lanes,
+           "slice_elements": args.serve_slice, "setup_s": {"meshes": mesh_s, "register": setup_s},
            "capacity_elements_per_s_initial": cap0, "sweep": []}
     nreq = args.serve_requests
     late = list(range(n_initial, len(cases)))
@@ -988,20 +1021,30 @@ def bench_serve(ft, torch, lib, stream, args, local, dist):
         for k in late:
             if admit(k):
                 admitted_mid.append(k)
+                live.append(k)  # the stream's next requests may pick it
+
+    def alone():
+        """Latency of one request per mesh on an idle server (best of two)."""
+        out = {}
+        for k in sorted(ids):
+            out[k] = min(srv.wait(submit(k, 0, rep % 2)) for rep in range(2))
+        return out
 
     for i, frac in enumerate((0.3, 0.6, 0.9, 1.1)):
         cap, mean_e = (cap0, mean0) if i == 0 else capacity()
         rate = frac * cap / mean_e
         live = sorted(ids)
-        lat, eps = _serve_stream(srv, rng, rate, nreq, submit, live, elems,
-                                 admit_at=nreq // 2 if i == 0 else None,
-                                 admit=admit_late if i == 0 else None)
+        lat, keys, eps = _serve_stream(srv, rng, rate, nreq, submit, live, elems,
+                                       admit_at=nreq // 2 if i == 0 else None,
+                                       admit=admit_late if i == 0 else None)
         if i == 0:
             res["capacity_elements_per_s"] = capacity()[0]  # all meshes admitted
-        p50, p99 = _percentiles(lat)
-        res["sweep"].append({"load": frac, "rate_per_s": rate, "requests": nreq,
-                             "meshes": len(live), "p50_ms": p50, "p99_ms": p99,
-                             "p99_over_p50": p99 / p50, "elements_per_s": float(eps)})
+            alone_ms = alone()
+            res["alone_ms"] = {"min": min(alone_ms.values()), "max": max(alone_ms.values())}
+        row = {"load": frac, "rate_per_s": rate, "requests": nreq, "meshes": len(live)}
+        row.update(_latency_stats(lat, keys, alone_ms))
+        row["elements_per_s"] = float(eps)
+        res["sweep"].append(row)
     res["admitted_mid_stream"] = len(admitted_mid)
     res["refused"] = len(refused)
     res["meshes"] = len(ids)
@@ -1031,11 +1074,11 @@ def bench_serve(ft, torch, lib, stream, args, local, dist):
         fsrv.wait(r)
     fp64_capacity = elems[live].sum() / (time.perf_counter() - t0)
     rate = 0.6 * fp64_capacity / elems[live].mean()
-    lat, eps = _serve_stream(fsrv, rng, rate, max(32, nreq // 2), fsubmit, live, elems)
-    p50, p99 = _percentiles(lat)
-    res["fp64_fast_server"] = {"capacity_elements_per_s": fp64_capacity, "load": 0.6,
-                               "p50_ms": p50, "p99_ms": p99, "p99_over_p50": p99 / p50,
-                               "elements_per_s": float(eps)}
+    falone = {k: min(fsrv.wait(fsubmit(k, 0, rep % 2)) for rep in range(2)) for k in live}
+    lat, keys, eps = _serve_stream(fsrv, rng, rate, max(32, nreq // 2), fsubmit, live, elems)
+    res["fp64_fast_server"] = {"capacity_elements_per_s": fp64_capacity, "load": 0.6}
+    res["fp64_fast_server"].update(_latency_stats(lat, keys, falone))
+    res["fp64_fast_server"]["elements_per_s"] = float(eps)
     res["capacity_mixed_over_fp64_fast"] = res["capacity_elements_per_s"] / fp64_capacity
     fsrv.close()
     del fids, ids, cases, srv, fsrv
@@ -1112,6 +1155,8 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=200,
                     help="requests per load level of the serving sweep")
     ap.add_argument("--serve-lanes", type=int, default=2)
+    ap.add_argument("--serve-slice", type=int, default=32768,
+                    help="elements of one request per launch of its lane")
     ap.add_argument("--t10-n", type=int, default=T10_N,
                     help="cells per side of the headline T10 block (60 = the benchmark size)")
     args = ap.parse_args()

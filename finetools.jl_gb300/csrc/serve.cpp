@@ -1,22 +1,21 @@
 // Serving loop: re-assembly requests on resident meshes, continuously batched
-// in rounds of bounded work.
+// on concurrent lanes, with bounded work per launch.
 //
 // A server keeps meshes resident on the device (connectivity, colouring, CSR
 // pattern, gather plan, block ring, coefficient buffer, matrix values) and
 // accepts requests that carry new per-element coefficients or new node
-// coordinates for one of them.  A worker thread runs the requests in rounds:
-// one round is one launch of the persistent assembly kernel (batch.cu) over
-// the whole GPU, holding the next slice of every request in flight -- a
-// bounded number of the mesh's element chunks (slice_elements) -- plus the
-// oldest waiting request of every mesh that has none in flight, up to a job
-// limit.  A small request completes in one round; a large one runs a slice
-// per round, so a request that arrives while a 2 M-element mesh is being
-// assembled waits at most one round, not the whole assembly, and a large
-// request alone still gets the whole GPU round after round.  Rounds are
-// queued on one stream (a request's slices run in order; its block ring
-// carries over from one slice to the next) with up to `depth` rounds in
-// flight, so the next round is queued while one runs.  Requests of one mesh
-// run in arrival order (at most one in flight per mesh).
+// coordinates for one of them.  A worker thread launches batches of the
+// persistent assembly kernel (batch.cu) on `lanes` CUDA streams.  When a lane
+// is free its next batch holds the next slice of every request running on it
+// and the oldest waiting request of every mesh with none running, up to a job
+// limit; a slice is at most slice_elements elements of a request's mesh, in
+// whole chunks, so a 2 M-element mesh is assembled over several launches of
+// its lane and cannot hold the lane for its whole assembly: requests that
+// arrive meanwhile join the lane's next launch or start on another lane
+// (continuous batching).  A request's slices run in order on its lane (its
+// block ring carries over from one launch to the next).  A launch covers
+// 1/(1 + lanes running) of the GPU: all of it when the others are idle.
+// Requests of one mesh run in arrival order (at most one running per mesh).
 //
 // Admission: a mesh is added only if the device memory it still needs to be
 // served (gather plan, block ring, coefficient and staging buffers) fits in
@@ -25,13 +24,13 @@
 // and the caller can remove a mesh and try again.  Meshes can be added and
 // removed while requests stream.
 //
-// Precision: rounds evaluate every request as the mixed-precision batch path.
-// A server set to FEGPU_FP64 or FEGPU_FP64_FAST instead runs each request by
-// itself through the single-call form on the context's stream (the FP64 forms
-// have no batched kernel), in arrival order.
+// Precision: the lanes evaluate every request as the mixed-precision batch
+// path.  A server set to FEGPU_FP64 or FEGPU_FP64_FAST instead runs each
+// request by itself through the single-call form on the context's stream (the
+// FP64 forms have no batched kernel), in arrival order.
 //
-// Completion times come from a host callback queued on the stream behind a
-// round's kernel (cudaLaunchHostFunc), so latencies include queueing, the
+// Completion times come from a host callback queued on the lane stream behind
+// the kernel (cudaLaunchHostFunc), so latencies include queueing, the
 // host-to-device copy of the request data and the assembly.
 #include <algorithm>
 #include <chrono>
@@ -57,7 +56,7 @@ double now_ms() {
   return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
 }
 
-// Page-locked host buffers recycled by size (request payloads, round staging).
+// Page-locked host buffers recycled by size (request payloads, lane staging).
 struct PinnedPool {
   std::mutex mu;
   std::multimap<size_t, void *> free_blocks;
@@ -97,14 +96,13 @@ constexpr int kReqPending = 0, kReqRunning = 1, kReqDone = 2, kReqFailed = 3,
 
 struct fegpu_server {
   fegpu_context *ctx = nullptr;
-  int depth = 2;                      // rounds in flight
+  int nlanes = 2;
   int max_jobs = 64;
   double wait_s = 5.0;
-  int64_t slice_elements = 262144;    // elements of one request per round
+  int64_t slice_elements = 32768;     // elements of one request per launch
   int precision = FEGPU_MIXED;
   int64_t mem_limit = 0;              // bytes the served meshes may hold (0: no limit)
   int64_t mem_held = 0;               // bytes they hold
-  cudaStream_t stream = nullptr;
 
   struct Mesh {
     fegpu_matrix *K = nullptr;
@@ -130,22 +128,24 @@ struct fegpu_server {
     double t_submit = 0, t_start = 0, t_done = 0;
     int state = kReqPending;
     int64_t next_chunk = 0;           // first chunk of its next slice
+    int lane = -1;                    // the lane its slices run on
   };
   std::unordered_map<int64_t, Request> requests;
   std::deque<int64_t> pending;        // waiting, arrival order
-  std::deque<int64_t> active;         // in flight (a slice per round), arrival order
+  std::deque<int64_t> active;         // running (more slices to come), arrival order
   int64_t next_id = 0;
 
-  struct Round {
+  struct Lane {
+    cudaStream_t stream = nullptr;
     DevBuf d_jobs, d_items, d_counters, d_next, d_status;
     void *h_jobs = nullptr, *h_items = nullptr;  // pinned staging (pool blocks)
     int *h_status = nullptr;
-    std::vector<int64_t> finishing;   // requests whose last slice is in this round
-    std::vector<int64_t> members;     // every request with a slice in this round
+    std::vector<int64_t> finishing;   // requests whose last slice is in this launch
+    std::vector<int64_t> members;     // every request with a slice in this launch
     bool busy = false;
     fegpu_server *srv = nullptr;
   };
-  std::vector<std::unique_ptr<Round>> rounds;
+  std::vector<std::unique_ptr<Lane>> lanes;
 
   PinnedPool pool;
   std::mutex mu;
@@ -163,16 +163,16 @@ int64_t chunks_of(const fegpu_server::Mesh &M) {
   return std::max<int64_t>(static_cast<int64_t>(M.K->dm->chunk_nodes.size()) - 1, 0);
 }
 
-void round_done(void *arg) {  // CUDA host callback: no CUDA calls here
-  auto *R = static_cast<fegpu_server::Round *>(arg);
+void lane_done(void *arg) {  // CUDA host callback: no CUDA calls here
+  auto *R = static_cast<fegpu_server::Lane *>(arg);
   fegpu_server *s = R->srv;
   const double t = now_ms();
   std::lock_guard<std::mutex> lock(s->mu);
   const bool ok = *R->h_status == 0;
-  // (a request failed by an earlier round may already be collected: look up)
+  // (a request failed by an earlier launch may already be collected: look up)
   if (!ok) {
-    // every request with a slice in this round is void; requests still in
-    // flight lose their remaining slices
+    // every request with a slice in this launch is void; requests still
+    // running lose their remaining slices
     for (int64_t id : R->members) {
       auto it = s->requests.find(id);
       if (it != s->requests.end() && it->second.state == kReqRunning) {
@@ -194,6 +194,15 @@ void round_done(void *arg) {  // CUDA host callback: no CUDA calls here
       s->meshes[it->second.mesh]->busy = false;
     }
   }
+  // the payloads of requests that ended here were copied by this launch or an
+  // earlier one of the lane: back to the pool for the next submissions
+  for (int64_t id : R->members) {
+    auto it = s->requests.find(id);
+    if (it != s->requests.end() && it->second.state >= kReqDone) {
+      s->pool.put(it->second.payload);
+      it->second.payload = nullptr;
+    }
+  }
   R->finishing.clear();
   R->members.clear();
   R->busy = false;
@@ -201,16 +210,18 @@ void round_done(void *arg) {  // CUDA host callback: no CUDA calls here
 }
 
 // Lane buffers grow by half again when they must grow, so that steady traffic
-// stops reallocating.
+// stops reallocating (cudaFree can stall behind the other lanes' work).
 void grow(DevBuf &b, size_t n) {
   if (n > b.bytes) b.alloc(std::max(n, b.bytes + b.bytes / 2));
 }
 
-// One round: uploads of the requests starting now, the items of every slice,
-// the launch, the completion callback (worker thread, no lock held).
-void launch_round(fegpu_server *s, fegpu_server::Round &R, const std::vector<int64_t> &ids,
-                  const std::vector<ChunkRange> &ranges, const std::vector<char> &starts) {
-  cudaStream_t st = s->stream;
+// One launch of a lane: uploads of the requests starting now, the items of
+// every slice, the kernel on `share` of the GPU, the completion callback
+// (worker thread, no lock held).
+void launch_lane(fegpu_server *s, fegpu_server::Lane &R, const std::vector<int64_t> &ids,
+                 const std::vector<ChunkRange> &ranges, const std::vector<char> &starts,
+                 double share) {
+  cudaStream_t st = R.stream;
   std::vector<BatchJob> jobs;
   std::vector<const fegpu_dofmap *> dms;
   for (size_t k = 0; k < ids.size(); ++k) {
@@ -238,8 +249,8 @@ void launch_round(fegpu_server *s, fegpu_server::Round &R, const std::vector<int
   const int ncount = build_batch_items(jobs, dms, 64u << 20, items, &ranges);
   const size_t smem = batch_smem_bytes(jobs, dms);
   const int nitems = static_cast<int>(items.size());
-  const int grid = batch_grid(s->ctx->num_sms, smem, nitems, 1.0);
-  // staging: the round's pinned blocks are free (its previous use is done)
+  const int grid = batch_grid(s->ctx->num_sms, smem, nitems, share);
+  // staging: the lane's pinned blocks are free (its previous launch is done)
   const size_t jb = sizeof(BatchJob) * jobs.size(), ib = sizeof(BatchItem) * items.size();
   s->pool.put(R.h_jobs);
   s->pool.put(R.h_items);
@@ -258,7 +269,7 @@ void launch_round(fegpu_server *s, fegpu_server::Round &R, const std::vector<int
   launch_batch_kernel(grid, smem, st, R.d_jobs.as<BatchJob>(), R.d_items.as<BatchItem>(), nitems,
                       R.d_next.as<int>(), R.d_counters.as<int>(), R.d_status.as<int>(), s->wait_s);
   FEGPU_CUDA(cudaMemcpyAsync(R.h_status, R.d_status.p, sizeof(int), cudaMemcpyDeviceToHost, st));
-  FEGPU_CUDA(cudaLaunchHostFunc(st, round_done, &R));
+  FEGPU_CUDA(cudaLaunchHostFunc(st, lane_done, &R));
 }
 
 // One FP64 request through the single-call form (worker thread, no lock held).
@@ -290,7 +301,8 @@ void run_fp64(fegpu_server *s, int64_t id) {
 void worker_main(fegpu_server *s) {
   cudaSetDevice(s->ctx->device);
   for (;;) {
-    fegpu_server::Round *R = nullptr;
+    fegpu_server::Lane *R = nullptr;
+    double share = 1.0;
     std::vector<int64_t> ids;
     std::vector<ChunkRange> ranges;
     std::vector<char> starts;
@@ -301,8 +313,15 @@ void worker_main(fegpu_server *s) {
       s->cv.wait(lock, [&] {
         if (s->stop) return true;
         if (s->hold || (s->pending.empty() && s->active.empty())) return false;
-        for (auto &x : s->rounds)
-          if (!x->busy) return true;
+        if (!s->pending.empty() && s->precision != FEGPU_MIXED) return true;
+        for (auto &x : s->lanes) {
+          if (x->busy) continue;
+          // a free lane with work: a request running on it, or one waiting
+          if (!s->pending.empty()) return true;
+          const int li = static_cast<int>(&x - &s->lanes[0]);
+          for (int64_t id : s->active)
+            if (s->requests[id].lane == li) return true;
+        }
         return false;
       });
       if (s->stop) return;
@@ -316,13 +335,28 @@ void worker_main(fegpu_server *s) {
         r.t_start = now_ms();
         ids.push_back(id);
       } else {
-        for (auto &x : s->rounds)
-          if (!x->busy) {
-            R = x.get();
+        // a free lane with a request running on it first (its next slice
+        // waits for that lane), else the first free lane
+        int li = -1;
+        for (int64_t id : s->active) {
+          const int l = s->requests[id].lane;
+          if (!s->lanes[l]->busy) {
+            li = l;
             break;
           }
-        // the next slice of every request in flight, then new requests: the
-        // oldest waiting request of each mesh that has none in flight
+        }
+        for (int l = 0; li < 0 && l < s->nlanes; ++l)
+          if (!s->lanes[l]->busy) li = l;
+        R = s->lanes[li].get();
+        // the launch takes its share of the GPU beside the lanes running now
+        // (all of it when they are idle): persistent blocks keep their SMs
+        // until the launch ends, so a launch sized for the whole GPU would
+        // make the next lane's launch wait for it
+        int running = 0;
+        for (auto &x : s->lanes) running += x->busy ? 1 : 0;
+        share = 1.0 / (1 + running);
+        // the next slice of every request running on this lane, then the
+        // oldest waiting request of each mesh with none running
         auto take_slice = [&](int64_t id, bool start) {
           auto &r = s->requests[id];
           const auto &M = *s->meshes[r.mesh];
@@ -338,13 +372,13 @@ void worker_main(fegpu_server *s) {
         };
         std::deque<int64_t> still;
         for (int64_t id : s->active) {
-          if (static_cast<int>(ids.size()) >= s->max_jobs) {
+          const auto &r = s->requests[id];
+          if (r.lane != li || static_cast<int>(ids.size()) >= s->max_jobs) {
             still.push_back(id);
             continue;
           }
           take_slice(id, false);
-          if (s->requests[id].next_chunk < chunks_of(*s->meshes[s->requests[id].mesh]))
-            still.push_back(id);
+          if (r.next_chunk < chunks_of(*s->meshes[r.mesh])) still.push_back(id);
         }
         std::deque<int64_t> rest;
         for (int64_t id : s->pending) {
@@ -355,6 +389,7 @@ void worker_main(fegpu_server *s) {
             r.state = kReqRunning;
             r.t_start = now_ms();
             r.next_chunk = 0;
+            r.lane = li;
             take_slice(id, true);
             if (r.next_chunk < chunks_of(M)) still.push_back(id);
           } else {
@@ -362,7 +397,7 @@ void worker_main(fegpu_server *s) {
           }
         }
         if (ids.empty()) {
-          // every waiting request waits for its mesh: sleep until a round ends
+          // every waiting request waits for its mesh: sleep until a launch ends
           s->cv.wait(lock);
           continue;
         }
@@ -380,11 +415,13 @@ void worker_main(fegpu_server *s) {
         auto &r = s->requests[ids[0]];
         r.state = kReqDone;
         r.t_done = now_ms();
+        s->pool.put(r.payload);  // copied (coordinates: the stream synchronized)
+        r.payload = nullptr;
         s->batches++;
         s->jobs_run++;
         s->cv.notify_all();
       } else {
-        launch_round(s, *R, ids, ranges, starts);
+        launch_lane(s, *R, ids, ranges, starts, share);
         std::lock_guard<std::mutex> lock(s->mu);
         s->batches++;
         s->jobs_run += static_cast<int64_t>(ids.size());
@@ -470,21 +507,25 @@ extern "C" {
 int fegpu_server_create(fegpu_context *ctx, int lanes, int max_jobs, fegpu_server **out) {
   return server_guard([&] {
     FEGPU_REQUIRE(ctx && out, "null handle");
-    FEGPU_REQUIRE(lanes >= 1 && lanes <= 16, "server: 1 to 16 rounds in flight");
+    FEGPU_REQUIRE(lanes >= 1 && lanes <= 16, "server: 1 to 16 lanes");
     FEGPU_REQUIRE(max_jobs >= 1, "server: max_jobs must be positive");
     FEGPU_CUDA(cudaSetDevice(ctx->device));
     auto s = std::make_unique<fegpu_server>();
     s->ctx = ctx;
-    s->depth = lanes;
+    s->nlanes = lanes;
     s->max_jobs = max_jobs;
-    FEGPU_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+    // lanes at the highest stream priority: their blocks are scheduled ahead
+    // of mesh admissions and other work on the context's stream
+    int least = 0, greatest = 0;
+    FEGPU_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
     for (int i = 0; i < lanes; ++i) {
-      auto R = std::make_unique<fegpu_server::Round>();
-      R->srv = s.get();
-      R->d_next.alloc(sizeof(int));
-      R->d_status.alloc(sizeof(int));
-      FEGPU_CUDA(cudaMallocHost(reinterpret_cast<void **>(&R->h_status), sizeof(int)));
-      s->rounds.push_back(std::move(R));
+      auto L = std::make_unique<fegpu_server::Lane>();
+      L->srv = s.get();
+      FEGPU_CUDA(cudaStreamCreateWithPriority(&L->stream, cudaStreamNonBlocking, greatest));
+      L->d_next.alloc(sizeof(int));
+      L->d_status.alloc(sizeof(int));
+      FEGPU_CUDA(cudaMallocHost(reinterpret_cast<void **>(&L->h_status), sizeof(int)));
+      s->lanes.push_back(std::move(L));
     }
     fegpu_server *raw = s.release();
     raw->worker = std::thread(worker_main, raw);
@@ -502,12 +543,12 @@ int fegpu_server_destroy(fegpu_server *s) {
     }
     if (s->worker.joinable()) s->worker.join();
     cudaSetDevice(s->ctx->device);
-    cudaStreamSynchronize(s->stream);
-    cudaStreamDestroy(s->stream);
-    for (auto &R : s->rounds) {
-      cudaFreeHost(R->h_status);
-      s->pool.put(R->h_jobs);
-      s->pool.put(R->h_items);
+    for (auto &L : s->lanes) {
+      cudaStreamSynchronize(L->stream);
+      cudaStreamDestroy(L->stream);
+      cudaFreeHost(L->h_status);
+      s->pool.put(L->h_jobs);
+      s->pool.put(L->h_items);
     }
     for (auto &kv : s->requests) s->pool.put(kv.second.payload);
     delete s;
@@ -706,6 +747,8 @@ int fegpu_server_cancel(fegpu_server *s, int64_t request_id) {
     if (it->second.state != kReqPending)
       throw Error{FEGPU_ERR_STATE, "server: the request is already running or done"};
     s->pending.erase(std::find(s->pending.begin(), s->pending.end(), request_id));
+    s->pool.put(it->second.payload);
+    it->second.payload = nullptr;
     it->second.state = kReqCancelled;
     it->second.t_done = now_ms();
     s->cv.notify_all();
@@ -728,7 +771,7 @@ int fegpu_server_wait(fegpu_server *s, int64_t request_id, double *latency_ms) {
     if (r.state == kReqFailed)
       throw Error{FEGPU_ERR_DEVICE,
                   s->worker_error.empty()
-                      ? "server: a work item of the request's round waited past its time limit"
+                      ? "server: a work item of the request's launch waited past its time limit"
                       : "server: " + s->worker_error};
   });
 }
@@ -750,8 +793,8 @@ int fegpu_server_drain(fegpu_server *s) {
                   "server: drain while launches are held");
     s->cv.wait(lock, [&] {
       if (!s->pending.empty() || !s->active.empty()) return false;
-      for (auto &R : s->rounds)
-        if (R->busy) return false;
+      for (auto &L : s->lanes)
+        if (L->busy) return false;
       for (auto &kv : s->requests)
         if (kv.second.state == kReqRunning) return false;
       return true;

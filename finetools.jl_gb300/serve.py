@@ -1,5 +1,6 @@
 """Serving loop: re-assembly requests on resident meshes (fegpu_server_* of
-include/fegpu.h), continuously batched onto the GPU in rounds of bounded work.
+include/fegpu.h), continuously batched onto the GPU on concurrent lanes, in slices of bounded
+work.
 
     server = AssemblyServer(lanes=2)
     mid, K = server.add_mesh("lin_elastic", femm, geom, u, IsotropicElementwise(E, nu))
@@ -10,7 +11,8 @@ include/fegpu.h), continuously batched onto the GPU in rounds of bounded work.
 Each request is evaluated as the mixed-precision batch path (or, with
 precision="fp64" / "fp64_fast", by the single-call FP64 form, one request at a
 time); a request's matrix does not depend on which other requests shared its
-rounds.  ``lanes`` is the number of rounds in flight.  A mesh is admitted only
+launches.  ``lanes`` is the number of CUDA streams launches run on; a request
+runs in slices of at most ``slice_elements`` elements on one lane.  A mesh is admitted only
 if the device memory it needs fits (and stays within memory_limit, if set).
 """
 from __future__ import annotations

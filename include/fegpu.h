@@ -309,18 +309,20 @@ int fegpu_batch_stats(fegpu_batch *b, int64_t *jobs, int64_t *items);
  * -- and accepts requests that carry new per-element coefficients
  * (FEGPU_REQUEST_COEF: the same layout as the coefficient the mesh was added
  * with) or new node coordinates (FEGPU_REQUEST_COORDS: nnodes x sdim,
- * column-major, as geom.values).  A worker thread runs them in rounds: one
- * launch of the persistent kernel over the whole GPU holds the next slice of
- * every request in flight (at most slice_elements of its mesh's elements,
- * fegpu_server_set_slice, default 262144) and the oldest waiting request of
- * every mesh with none in flight, up to max_jobs; `lanes` rounds may be in
- * flight (the next queued while one runs).  A request that arrives during a
- * large assembly therefore waits at most a round, and a large request alone
- * has the whole GPU.  Requests of one mesh complete in submission order; a
+ * column-major, as geom.values).  A worker thread launches the persistent
+ * kernel on `lanes` CUDA streams.  When a lane is free its next launch holds
+ * the next slice of every request running on it (a slice: at most
+ * slice_elements of the mesh's elements in whole chunks,
+ * fegpu_server_set_slice, default 32768) and the oldest waiting request of
+ * every mesh with none running, up to max_jobs; a launch covers 1/(1 + lanes
+ * running) of the GPU (all of it when the other lanes are idle).  A large
+ * request therefore runs over several launches of its lane, and requests that
+ * arrive meanwhile start on another lane or join its next launch.  Requests of
+ * one mesh complete in submission order; a
  * request's result is the mesh's matrix (values on the device, read with
  * fegpu_matrix_copy_values before the mesh's next request completes).  Every
  * request is evaluated as the batch path (FEGPU_MIXED) and its matrix does
- * not depend on what else shared its rounds.  Latency = completion (host
+ * not depend on what else shared its launches.  Latency = completion (host
  * callback behind the kernel) - submit.  The data passed to
  * fegpu_server_submit is copied; the matrices must outlive the server; a
  * coordinates request also changes the femm's geometry. */
@@ -367,7 +369,7 @@ int fegpu_server_drain(fegpu_server *s);
 /* hold = 1: no new launches (requests accumulate, e.g. during maintenance or
  * to admit a burst at once); hold = 0: resume */
 int fegpu_server_hold(fegpu_server *s, int hold);
-/* rounds launched, request slices run, requests waiting */
+/* launches, request slices run, requests waiting */
 int fegpu_server_stats(fegpu_server *s, int64_t *batches, int64_t *jobs, int64_t *pending);
 /* free and total device memory */
 int fegpu_server_memory(fegpu_server *s, int64_t *free_bytes, int64_t *total_bytes);

@@ -142,9 +142,10 @@ def test_server_rejects_bad_requests(ft):
 
 
 def test_large_request_in_slices_equals_single_call(ft):
-    """A request cut into several rounds (a few element chunks per round, its
-    block ring carried from one round to the next) gives the single-call
-    matrix bit for bit, also with other requests sharing its rounds."""
+    """A request cut into several slices (one element chunk per launch of its
+    lane, its block ring carried from one launch to the next) gives the
+    single-call matrix bit for bit, also with other requests sharing its
+    launches."""
     cases = _meshes(ft)
     big = dict(cases[1])
     fens, fes = ft.nearest_block("T10", 60000, seed=77)
@@ -153,7 +154,7 @@ def test_large_request_in_slices_equals_single_call(ft):
     E = fes.count()
     big.update(femm=femm, geom=ft.NodalField(fens.xyz), u=_field(ft, fens.count(), 3), E=E,
                cf=ft.IsotropicElementwise(rng.lognormal(np.log(70e9), 1.0, E), np.full(E, 0.3)))
-    srv = ft.AssemblyServer(lanes=2, max_jobs=8, slice_elements=1)  # one chunk per round
+    srv = ft.AssemblyServer(lanes=2, max_jobs=8, slice_elements=1)  # one chunk per launch
     mid, M = srv.add_mesh(big["form"], big["femm"], big["geom"], big["u"], big["cf"])
     small = [srv.add_mesh(c["form"], c["femm"], c["geom"], c["u"], c["cf"]) for c in cases[2:4]]
     cf, data = _new_coef(ft, big, rng)
@@ -170,7 +171,7 @@ def test_large_request_in_slices_equals_single_call(ft):
     got = M.values()
     got_small = [Ms.values() for _, Ms in small]
     srv.close()
-    assert nchunks > 2 and st["batches"] >= nchunks  # the big request took several rounds
+    assert nchunks > 2 and st["batches"] >= nchunks  # the big request took several launches
     assert np.array_equal(got, _single_mixed(ft, big, cf))
     for v, c, (cfs, _) in zip(got_small, cases[2:4], scf):
         assert np.array_equal(v, _single_mixed(ft, c, cfs))
@@ -178,7 +179,7 @@ def test_large_request_in_slices_equals_single_call(ft):
 
 def test_mesh_admitted_while_requests_stream(ft):
     """A mesh is added while requests on the others are in flight; its own
-    requests then run in the same rounds, and every result equals the single
+    requests then run beside theirs, and every result equals the single
     call."""
     cases = _meshes(ft)
     srv = ft.AssemblyServer(lanes=2, max_jobs=8, slice_elements=2000)
