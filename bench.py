@@ -513,8 +513,8 @@ def run_ours(args):
     # every host buffer written by the pipelined loop holds the assembled
     # values (a strided sample against the device copy)
     ref = K.values()[::97]
-    e2e_check = all(bool(np.array_equal(vals_h[i][::97], ref))
-                    for i in range(min(2, args.steps + args.warmup)))
+    written = {i & 1 for i in range(args.warmup)} | {i & 1 for i in range(args.steps)}
+    e2e_check = all(bool(np.array_equal(vals_h[i][::97], ref)) for i in sorted(written))
     lib.nat.check(lib.L.fegpu_matrix_destroy(k2.value))
     lib.stats(reset=True)
 

@@ -26,7 +26,8 @@ ASM_SPARSE, ASM_SPARSE_SYMM, ASM_SPARSE_DIAG, ASM_HRZ_LUMPING_SYMM = 0, 1, 2, 3
 EXPORTS = [
     "fegpu_last_error", "fegpu_context_create", "fegpu_context_destroy",
     "fegpu_context_synchronize", "fegpu_context_stream", "fegpu_context_timing",
-    "fegpu_context_kernel_stats", "fegpu_context_device_checks", "fegpu_femm_create", "fegpu_femm_destroy",
+    "fegpu_context_kernel_stats", "fegpu_context_device_checks", "fegpu_selftest_soft_add",
+    "fegpu_femm_create", "fegpu_femm_destroy",
     "fegpu_femm_set_geometry", "fegpu_femm_set_axisymmetric", "fegpu_femm_colors", "fegpu_dofmap_create",
     "fegpu_dofmap_destroy", "fegpu_dofmap_copy_pattern", "fegpu_matrix_create",
     "fegpu_matrix_destroy", "fegpu_matrix_set_symmetric_assembly", "fegpu_bilform_diffusion", "fegpu_bilform_lin_elastic",
@@ -79,6 +80,8 @@ def load(path: str = LIBPATH):
         "fegpu_context_timing": ([vp, i32], i32),
         "fegpu_context_kernel_stats": ([vp, C.POINTER(C.c_double), p64, i32], i32),
         "fegpu_context_device_checks": ([vp, C.POINTER(C.c_int)], i32),
+        "fegpu_selftest_soft_add": ([vp, C.c_int64, C.c_uint64, C.POINTER(C.c_int64),
+                                     C.POINTER(C.c_int64)], i32),
         "fegpu_femm_create": ([vp, i32, i64, vp, i64, i32, vp, vp, vp, d, pp], i32),
         "fegpu_femm_destroy": ([vp], i32),
         "fegpu_femm_set_geometry": ([vp, i32, vp], i32),

@@ -304,3 +304,94 @@ void run_exact(fegpu_dofmap *dm, int form, KArgs &a, bool symmetric) {
 }
 
 }  // namespace fegpu
+
+// ---- device self-test of the integer-unit addition ----------------------
+namespace fegpu {
+namespace {
+
+__device__ __forceinline__ uint64_t st_mix(uint64_t z) {  // splitmix64 finaliser
+  z += 0x9e3779b97f4a7c15ull;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+
+__device__ __forceinline__ double st_make(uint64_t sign, uint64_t ex, uint64_t frac) {
+  return sf_double((sign << 63) | (ex << 52) | (frac & 0x000fffffffffffffull));
+}
+
+// operand pairs of four kinds (uniform bit patterns; exponent differences
+// 0..70; near-cancellations; ties to even), sf_add against __dadd_rn
+__global__ void k_selftest_soft_add(uint64_t seed, int64_t n, unsigned long long *bad,
+                                    unsigned long long *first) {
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const uint64_t r1 = st_mix(seed + 4 * static_cast<uint64_t>(i));
+    const uint64_t r2 = st_mix(seed + 4 * static_cast<uint64_t>(i) + 1);
+    const uint64_t r3 = st_mix(seed + 4 * static_cast<uint64_t>(i) + 2);
+    double x, y;
+    switch (i & 3) {
+      case 0:
+        x = sf_double(r1);
+        y = sf_double(r2);
+        break;
+      case 1: {
+        const uint64_t ex = 1 + r3 % 2046, d = (r3 >> 20) % 71;
+        x = st_make(r1 >> 63, ex, r1);
+        y = st_make(r2 >> 63, ex > d ? ex - d : 1, r2);
+        break;
+      }
+      case 2: {
+        x = st_make(r1 >> 63, 1 + r3 % 2046, r1);
+        const int64_t k = static_cast<int64_t>((r3 >> 20) % 9) - 4;
+        y = -sf_double(sf_bits(x) + static_cast<uint64_t>(k));
+        break;
+      }
+      default: {
+        const uint64_t ex = 60 + r3 % 1900, d = 1 + (r3 >> 20) % 56;
+        x = st_make(r1 >> 63, ex, r1 & ~0xffull);
+        y = st_make(r2 >> 63, ex - d,
+                    (r2 & 0x000ffffffffff000ull) | (1ull << ((r3 >> 40) % 12)));
+        break;
+      }
+    }
+    const double s = sf_add(x, y), h = __dadd_rn(x, y);
+    const bool same = sf_bits(s) == sf_bits(h) || (isnan(s) && isnan(h));
+    if (!same) {
+      atomicAdd(bad, 1ull);
+      atomicMin(first, static_cast<unsigned long long>(i));
+    }
+  }
+}
+
+}  // namespace
+}  // namespace fegpu
+
+extern "C" int fegpu_selftest_soft_add(fegpu_context *ctx, int64_t n, uint64_t seed,
+                                       int64_t *mismatches, int64_t *first) {
+  using namespace fegpu;
+  try {
+    FEGPU_REQUIRE(ctx && mismatches && n >= 0, "null handle or negative count");
+    FEGPU_CUDA(cudaSetDevice(ctx->device));
+    DevBuf d;
+    d.alloc(2 * sizeof(unsigned long long));
+    const unsigned long long init[2] = {0ull, ~0ull};
+    FEGPU_CUDA(cudaMemcpyAsync(d.p, init, sizeof(init), cudaMemcpyHostToDevice, ctx->stream));
+    auto *p = d.as<unsigned long long>();
+    if (n > 0) {
+      const int grid = static_cast<int>(std::min<int64_t>((n + 255) / 256, 8 * ctx->num_sms));
+      k_selftest_soft_add<<<grid, 256, 0, ctx->stream>>>(seed, n, p, p + 1);
+      FEGPU_CUDA(cudaGetLastError());
+      ctx->launches += 1;
+    }
+    unsigned long long out[2];
+    FEGPU_CUDA(cudaMemcpyAsync(out, d.p, sizeof(out), cudaMemcpyDeviceToHost, ctx->stream));
+    FEGPU_CUDA(cudaStreamSynchronize(ctx->stream));
+    *mismatches = static_cast<int64_t>(out[0]);
+    if (first) *first = out[0] ? static_cast<int64_t>(out[1]) : -1;
+    return FEGPU_OK;
+  } catch (const Error &e) {
+    set_error(e.msg);
+    return e.code;
+  }
+}

@@ -33,13 +33,27 @@
 #pragma once
 
 #include "elements.cuh"
+#include "softf64.cuh"
 
 namespace fegpu {
 
 constexpr int kExactThreads = 256;
 
+// separately rounded FP64 products and sums on the FP64 unit (xm, xa), and
+// sums over the quadrature points (xs<SOFT>): with SOFT on the integer units
+// (sf_add, bit-identical to the FP64 unit's sum), so that GB300's narrow FP64
+// pipe and its integer issue share the element blocks.  That pays where the
+// block kernel keeps enough warps per SM to cover the integer chains' latency
+// (T10 elasticity, 2 CTAs of 256 threads: 35.3 -> 31.3 ms at 60^3); with one
+// CTA per SM (H20) or sums that are all point sums (H8 diffusion) the FP64
+// unit alone is faster.
 __device__ __forceinline__ double xm(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ double xa(double a, double b) { return __dadd_rn(a, b); }
+template <bool SOFT>
+__device__ __forceinline__ double xs(double a, double b) {
+  if constexpr (SOFT) return sf_add(a, b);
+  else return __dadd_rn(a, b);
+}
 
 // values kept per (element, point, node) for the block phase: the weighted
 // gradients (diffusion), or the nonzeros of the node's three DB columns
@@ -95,6 +109,7 @@ template <int ET, int FORM>
 __global__ void __launch_bounds__(kExactThreads) k_blocks_exact(const KArgs a) {
   constexpr int NNE = ElemT<ET>::NNE, MDIM = ElemT<ET>::MDIM;
   constexpr bool ELAST = FORM == F_ELAST_ISO || FORM == F_ELAST_GEN;
+  constexpr bool SOFT = ELAST && ET == FEGPU_T10;  // point sums on the integer units
   constexpr int NDN = ELAST ? 3 : 1;
   constexpr int BS = NDN * NDN;
   constexpr int NBLK = NNE * (NNE + 1) / 2;
@@ -218,12 +233,12 @@ __global__ void __launch_bounds__(kExactThreads) k_blocks_exact(const KArgs a) {
           if constexpr (FORM == F_DIFF_ISO) {
             // Ke[a][b] += g[a][p] * av[b][p], one p at a time
 #pragma unroll
-            for (int m = 0; m < MDIM; ++m) s = xa(s, xm(x[m], y[m]));
+            for (int m = 0; m < MDIM; ++m) s = xs<SOFT>(s, xm(x[m], y[m]));
           } else {
             double acc = xm(x[0], y[0]);
 #pragma unroll
             for (int m = 1; m < MDIM; ++m) acc = xa(acc, xm(x[m], y[m]));
-            s = xa(s, acc);
+            s = xs<SOFT>(s, acc);
           }
         }
         out[0] = s;
@@ -244,16 +259,16 @@ __global__ void __launch_bounds__(kExactThreads) k_blocks_exact(const KArgs a) {
             const double Px = v[0], Py = v[1], Pz = v[2];
             const double Qx = v[3], Qy = v[4], Qz = v[5];
             const double Sx = v[6], Sy = v[7], Sz = v[8];
-            K[0][0] = xa(K[0][0], xa(xa(xm(ax, Px), xm(ay, Sy)), xm(az, Sz)));
-            K[0][1] = xa(K[0][1], xa(xm(ax, Qy), xm(ay, Sx)));
-            K[0][2] = xa(K[0][2], xa(xm(ax, Qz), xm(az, Sx)));
-            K[1][1] = xa(K[1][1], xa(xa(xm(ay, Py), xm(ax, Sx)), xm(az, Sz)));
-            K[1][2] = xa(K[1][2], xa(xm(ay, Qz), xm(az, Sy)));
-            K[2][2] = xa(K[2][2], xa(xa(xm(az, Pz), xm(ax, Sx)), xm(ay, Sy)));
+            K[0][0] = xs<SOFT>(K[0][0], xa(xa(xm(ax, Px), xm(ay, Sy)), xm(az, Sz)));
+            K[0][1] = xs<SOFT>(K[0][1], xa(xm(ax, Qy), xm(ay, Sx)));
+            K[0][2] = xs<SOFT>(K[0][2], xa(xm(ax, Qz), xm(az, Sx)));
+            K[1][1] = xs<SOFT>(K[1][1], xa(xa(xm(ay, Py), xm(ax, Sx)), xm(az, Sz)));
+            K[1][2] = xs<SOFT>(K[1][2], xa(xm(ay, Qz), xm(az, Sy)));
+            K[2][2] = xs<SOFT>(K[2][2], xa(xa(xm(az, Pz), xm(ax, Sx)), xm(ay, Sy)));
             if (!diag) {
-              K[1][0] = xa(K[1][0], xa(xm(ay, Qx), xm(ax, Sy)));
-              K[2][0] = xa(K[2][0], xa(xm(az, Qx), xm(ax, Sz)));
-              K[2][1] = xa(K[2][1], xa(xm(az, Qy), xm(ay, Sz)));
+              K[1][0] = xs<SOFT>(K[1][0], xa(xm(ay, Qx), xm(ax, Sy)));
+              K[2][0] = xs<SOFT>(K[2][0], xa(xm(az, Qx), xm(ax, Sz)));
+              K[2][1] = xs<SOFT>(K[2][1], xa(xm(az, Qy), xm(ay, Sz)));
             }
           } else {
             // v[3 m + j] = DB[m][(b,j)]; column (a,x): rows 0, 3, 4;
@@ -261,13 +276,13 @@ __global__ void __launch_bounds__(kExactThreads) k_blocks_exact(const KArgs a) {
 #pragma unroll
             for (int j = 0; j < 3; ++j) {
               if (!diag || j >= 0) {
-                K[0][j] = xa(K[0][j], xa(xa(xm(ax, v[j]), xm(ay, v[9 + j])), xm(az, v[12 + j])));
+                K[0][j] = xs<SOFT>(K[0][j], xa(xa(xm(ax, v[j]), xm(ay, v[9 + j])), xm(az, v[12 + j])));
               }
               if (!diag || j >= 1) {
-                K[1][j] = xa(K[1][j], xa(xa(xm(ay, v[3 + j]), xm(ax, v[9 + j])), xm(az, v[15 + j])));
+                K[1][j] = xs<SOFT>(K[1][j], xa(xa(xm(ay, v[3 + j]), xm(ax, v[9 + j])), xm(az, v[15 + j])));
               }
               if (!diag || j >= 2) {
-                K[2][j] = xa(K[2][j], xa(xa(xm(az, v[6 + j]), xm(ax, v[12 + j])), xm(ay, v[15 + j])));
+                K[2][j] = xs<SOFT>(K[2][j], xa(xa(xm(az, v[6 + j]), xm(ax, v[12 + j])), xm(ay, v[15 + j])));
               }
             }
           }

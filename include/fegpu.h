@@ -106,6 +106,14 @@ int fegpu_context_timing(fegpu_context *ctx, int enable);
  * returns FEGPU_ERR_DEVICE naming it.  Regular builds compile the checks
  * away. */
 int fegpu_context_device_checks(fegpu_context *ctx, int *enabled);
+/* Self-test of the integer-unit FP64 addition that the reference-order path
+ * uses for part of its sums (no reference counterpart): n operand pairs
+ * (uniform bit patterns, close exponents, near-cancellations, ties to even)
+ * from the seed, each summed by the routine and by the FP64 unit on the
+ * device; the number of results that differ in any bit (0 expected) and the
+ * index of the first (-1 if none). */
+int fegpu_selftest_soft_add(fegpu_context *ctx, int64_t n, uint64_t seed, int64_t *mismatches,
+                            int64_t *first);
 int fegpu_context_kernel_stats(fegpu_context *ctx, double *kernel_ms, int64_t *launches,
                                int reset);
 

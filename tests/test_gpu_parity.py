@@ -1294,3 +1294,19 @@ def test_axisymmetric_forms(ft, O, kats, form):
     x = np.random.default_rng(5).uniform(-1, 1, K.shape[0])
     assert np.linalg.norm((K32 - K) @ x) <= MIXED_TOL * np.linalg.norm(K @ x)
     mixed_gate(K32, K)
+
+
+def test_integer_unit_addition_matches_fp64_unit(ft):
+    """sf_add (the T10 elasticity kernel's point sums on the integer units)
+    against the FP64 unit's __dadd_rn on the device: 4 million operand pairs
+    of four kinds (uniform bit patterns, exponent differences 0..70,
+    near-cancellations, ties to even), every result equal in every bit."""
+    import ctypes as C
+    from importlib import import_module
+    nat = import_module(ft.__name__ + "._native")
+    L = nat.load()
+    bad, first = C.c_int64(), C.c_int64()
+    for seed in (1, 20261204):
+        nat.check(L.fegpu_selftest_soft_add(nat.context(0), 4_000_000, seed, C.byref(bad),
+                                            C.byref(first)))
+        assert bad.value == 0 and first.value == -1, (seed, bad.value, first.value)
