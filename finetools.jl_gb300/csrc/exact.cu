@@ -212,11 +212,7 @@ int exact_tile(int etype, int form, int npts) {
   const size_t two = exact_layout(nne, mdim, npts, 2, form).total;
   const size_t per = two - one;
   const size_t fixed = one - per;
-  // two CTAs per SM (one for the largest elements); three for T10 elasticity,
-  // whose point sums run on the integer units and want more warps to cover
-  // their latency (16 elements per tile: 30.3 against 31.3 ms at 60^3)
-  const bool soft = etype == FEGPU_T10 && (form == F_ELAST_ISO || form == F_ELAST_GEN);
-  const size_t budget = per > 24 * 1024 ? 220 * 1024 : (soft ? 72 * 1024 : 110 * 1024);
+  const size_t budget = per > 24 * 1024 ? 220 * 1024 : 110 * 1024;
   int te = static_cast<int>((budget - std::min(budget, fixed)) / std::max<size_t>(per, 1));
   te = std::max(1, std::min(te, 64));
   // FEGPU_EXACT_TILE fixes the elements per tile (tuning; capped by the
