@@ -622,8 +622,10 @@ def run_ours(args):
                                      "FP64 FMA instructions per second)",
                       "dgemm_tflops": fp64_peak,
                       "instructions_per_assembly": ops,
-                      "note": "every instruction a separately rounded FP64 multiply or add "
-                              "(the reference's roundings)"},
+                      "note": "operations of the reference's order, every one a separately "
+                              "rounded FP64 multiply or add; the element blocks' sums over the "
+                              "points run on the integer units (bit-identical IEEE additions), "
+                              "so the rate counts them though the FP64 pipe does not issue them"},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "elements/s", "h2d_bytes_per_step": N * 3 * 8,
                 "d2h_bytes_per_step": nnz * 8,
