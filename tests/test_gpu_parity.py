@@ -964,14 +964,18 @@ def test_async_export_pipeline(ft):
         assert np.allclose(bufs[i], sc * bufs[0], rtol=1e-12, atol=1e-13 * sc * top)
 
 
-@pytest.mark.parametrize("et", ["H20", "T10", "H8", "T4"])
+@pytest.mark.parametrize("et", ["H20", "T10", "H8", "T4", "H20_mirrored"])
 def test_mixed_tensor_core_blocks(ft, et, monkeypatch):
     """The tensor-core element blocks (tcgen05 kind::tf32, split hi/lo
     operands) against the FP64 path, beside the FP32-pipe blocks: both within
-    the mixed tolerance, exactly symmetric, and not the same arithmetic."""
+    the mixed tolerance, exactly symmetric, and not the same arithmetic.  The
+    mirrored mesh (every det J < 0) takes the two-operand products instead of
+    the symmetric rank-K ones."""
     rng = np.random.default_rng(9)
-    if et == "H20":
+    if et.startswith("H20"):
         fens, fes, _ = ft.h20_elastic_mesh(n=4, distort_fraction=0.05)
+        if et == "H20_mirrored":
+            fens.xyz = fens.xyz * np.array([-1.0, 1.0, 1.0])
         r = ft.GaussRule(3, 3)
     elif et == "T10":
         fens, fes = ft.t10_elastic_mesh(n=3)
