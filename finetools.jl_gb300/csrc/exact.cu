@@ -212,7 +212,12 @@ int exact_tile(int etype, int form, int npts) {
   const size_t two = exact_layout(nne, mdim, npts, 2, form).total;
   const size_t per = two - one;
   const size_t fixed = one - per;
-  const size_t budget = per > 24 * 1024 ? 220 * 1024 : 110 * 1024;
+  // two CTAs per SM, or one for elements whose blocks take more than 24 KB of
+  // shared memory each; H20 elasticity, whose point sums run on the integer
+  // units, takes one element per tile and three CTAs per SM instead (more
+  // warps to cover the integer chains' latency: 31.3 against 40.0 ms at 40^3)
+  const bool soft_wide = etype == FEGPU_H20 && (form == F_ELAST_ISO || form == F_ELAST_GEN);
+  const size_t budget = per > 24 * 1024 ? (soft_wide ? 72 * 1024 : 220 * 1024) : 110 * 1024;
   int te = static_cast<int>((budget - std::min(budget, fixed)) / std::max<size_t>(per, 1));
   te = std::max(1, std::min(te, 64));
   // FEGPU_EXACT_TILE fixes the elements per tile (tuning; capped by the

@@ -43,10 +43,12 @@ constexpr int kExactThreads = 256;
 // sums over the quadrature points (xs<SOFT>): with SOFT on the integer units
 // (sf_add, bit-identical to the FP64 unit's sum), so that GB300's narrow FP64
 // pipe and its integer issue share the element blocks.  That pays where the
-// block kernel keeps enough warps per SM to cover the integer chains' latency
-// (T10 elasticity, 2 CTAs of 256 threads: 35.3 -> 31.3 ms at 60^3); with one
-// CTA per SM (H20) or sums that are all point sums (H8 diffusion) the FP64
-// unit alone is faster.
+// block kernel keeps enough warps per SM to cover the integer chains' latency:
+// T10 elasticity, two CTAs of 256 threads (35.3 -> 31.3 ms at 60^3), and H20
+// elasticity with one element per tile, three CTAs per SM (34.9 -> 31.3 ms at
+// 40^3; with three elements per tile and one CTA per SM the integer sums
+// made it slower, 40.0 ms).  Where the sums are all point sums (H8
+// diffusion) the FP64 unit alone is faster.
 __device__ __forceinline__ double xm(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ double xa(double a, double b) { return __dadd_rn(a, b); }
 template <bool SOFT>
@@ -109,7 +111,7 @@ template <int ET, int FORM>
 __global__ void __launch_bounds__(kExactThreads) k_blocks_exact(const KArgs a) {
   constexpr int NNE = ElemT<ET>::NNE, MDIM = ElemT<ET>::MDIM;
   constexpr bool ELAST = FORM == F_ELAST_ISO || FORM == F_ELAST_GEN;
-  constexpr bool SOFT = ELAST && ET == FEGPU_T10;  // point sums on the integer units
+  constexpr bool SOFT = ELAST && (ET == FEGPU_T10 || ET == FEGPU_H20);  // point sums on the integer units
   constexpr int NDN = ELAST ? 3 : 1;
   constexpr int BS = NDN * NDN;
   constexpr int NBLK = NNE * (NNE + 1) / 2;
