@@ -213,11 +213,15 @@ int exact_tile(int etype, int form, int npts) {
   const size_t per = two - one;
   const size_t fixed = one - per;
   // two CTAs per SM, or one for elements whose blocks take more than 24 KB of
-  // shared memory each; H20 elasticity, whose point sums run on the integer
-  // units, takes one element per tile and three CTAs per SM instead (more
-  // warps to cover the integer chains' latency: 31.3 against 40.0 ms at 40^3)
-  const bool soft_wide = etype == FEGPU_H20 && (form == F_ELAST_ISO || form == F_ELAST_GEN);
-  const size_t budget = per > 24 * 1024 ? (soft_wide ? 72 * 1024 : 220 * 1024) : 110 * 1024;
+  // shared memory each.  T10 and H20 elasticity, whose point sums run on the
+  // integer units, take three CTAs per SM instead (more warps to cover the
+  // integer chains' latency): 16 T10 elements per tile (T10 60^3: 30.3
+  // against 31.4 ms with 26 and two CTAs), one H20 element (H20 40^3: 31.2
+  // against 40.0 ms with three and one CTA)
+  const bool elast = form == F_ELAST_ISO || form == F_ELAST_GEN;
+  size_t budget = per > 24 * 1024 ? 220 * 1024 : 110 * 1024;
+  if (elast && etype == FEGPU_T10) budget = 68 * 1024;
+  if (elast && etype == FEGPU_H20) budget = 72 * 1024;
   int te = static_cast<int>((budget - std::min(budget, fixed)) / std::max<size_t>(per, 1));
   te = std::max(1, std::min(te, 64));
   // FEGPU_EXACT_TILE fixes the elements per tile (tuning; capped by the

@@ -261,12 +261,14 @@ __global__ void __launch_bounds__(kExactThreads) k_blocks_exact(const KArgs a) {
             const double Px = v[0], Py = v[1], Pz = v[2];
             const double Qx = v[3], Qy = v[4], Qz = v[5];
             const double Sx = v[6], Sy = v[7], Sz = v[8];
-            K[0][0] = xs<SOFT>(K[0][0], xa(xa(xm(ax, Px), xm(ay, Sy)), xm(az, Sz)));
+            // (the first sum of each diagonal entry's three products on the
+            // integer units too: 30.2 -> 29.4 ms at T10 60^3)
+            K[0][0] = xs<SOFT>(K[0][0], xa(xs<SOFT>(xm(ax, Px), xm(ay, Sy)), xm(az, Sz)));
             K[0][1] = xs<SOFT>(K[0][1], xa(xm(ax, Qy), xm(ay, Sx)));
             K[0][2] = xs<SOFT>(K[0][2], xa(xm(ax, Qz), xm(az, Sx)));
-            K[1][1] = xs<SOFT>(K[1][1], xa(xa(xm(ay, Py), xm(ax, Sx)), xm(az, Sz)));
+            K[1][1] = xs<SOFT>(K[1][1], xa(xs<SOFT>(xm(ay, Py), xm(ax, Sx)), xm(az, Sz)));
             K[1][2] = xs<SOFT>(K[1][2], xa(xm(ay, Qz), xm(az, Sy)));
-            K[2][2] = xs<SOFT>(K[2][2], xa(xa(xm(az, Pz), xm(ax, Sx)), xm(ay, Sy)));
+            K[2][2] = xs<SOFT>(K[2][2], xa(xs<SOFT>(xm(az, Pz), xm(ax, Sx)), xm(ay, Sy)));
             if (!diag) {
               K[1][0] = xs<SOFT>(K[1][0], xa(xm(ay, Qx), xm(ax, Sy)));
               K[2][0] = xs<SOFT>(K[2][0], xa(xm(az, Qx), xm(ax, Sz)));
