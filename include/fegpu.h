@@ -97,7 +97,7 @@ int fegpu_context_stream(fegpu_context *ctx, void **stream);
  * (ms) and the number of kernels the library launched, and resets them when
  * reset != 0. */
 int fegpu_context_timing(fegpu_context *ctx, int enable);
-/* Whether this build checks device indices (no reference counterpart: the
+/* Whether the loaded library checks device indices (no reference counterpart: the
  * reference's assemble! bounds-checks every DOF, src/AssemblyModule.jl:
  * 519-524).  A library built with FEGPU_DEVICE_CHECKS (build.py
  * --device-checks, libfegpu_checked.so) checks in its kernels the node
