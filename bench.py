@@ -1157,7 +1157,7 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=200,
                     help="requests per load level of the serving sweep")
     ap.add_argument("--serve-lanes", type=int, default=2)
-    ap.add_argument("--serve-slice", type=int, default=32768,
+    ap.add_argument("--serve-slice", type=int, default=16384,
                     help="elements of one request per launch of its lane")
     ap.add_argument("--t10-n", type=int, default=T10_N,
                     help="cells per side of the headline T10 block (60 = the benchmark size)")

@@ -99,7 +99,7 @@ struct fegpu_server {
   int nlanes = 2;
   int max_jobs = 64;
   double wait_s = 5.0;
-  int64_t slice_elements = 32768;     // elements of one request per launch
+  int64_t slice_elements = 16384;     // elements of one request per launch
   int precision = FEGPU_MIXED;
   int64_t mem_limit = 0;              // bytes the served meshes may hold (0: no limit)
   int64_t mem_held = 0;               // bytes they hold

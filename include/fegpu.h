@@ -321,7 +321,7 @@ int fegpu_batch_stats(fegpu_batch *b, int64_t *jobs, int64_t *items);
  * kernel on `lanes` CUDA streams.  When a lane is free its next launch holds
  * the next slice of every request running on it (a slice: at most
  * slice_elements of the mesh's elements in whole chunks,
- * fegpu_server_set_slice, default 32768) and the oldest waiting request of
+ * fegpu_server_set_slice, default 16384) and the oldest waiting request of
  * every mesh with none running, up to max_jobs; a launch covers 1/(1 + lanes
  * running) of the GPU (all of it when the other lanes are idle).  A large
  * request therefore runs over several launches of its lane, and requests that
