@@ -45,7 +45,7 @@ struct BatchItem {
 };
 
 constexpr int kBatchThreads = 256;
-constexpr int kBatchGatherNodes = 64;
+constexpr int kBatchGatherNodes = 32;
 // dynamic shared memory limit of the kernel (227 KB per CTA less its static part)
 constexpr size_t kBatchMaxSmem = 227 * 1024 - 1024;
 // coefficient kind of a dot job whose (matrix) coefficient is carried by cab/cdiag
