@@ -125,7 +125,7 @@ def _field(ft, n, ndn):
 @pytest.mark.parametrize("et,n,rule", [("H8", 4, ("G", 3, 2)), ("H20", 3, ("G", 3, 3)),
                                        ("T4", 3, ("T", 1)), ("T10", 3, ("T", 4)),
                                        ("H8", 3, ("G", 3, 3)), ("T10", 2, ("T", 5))])
-@pytest.mark.parametrize("coef", ["iso", "general", "per_element"])
+@pytest.mark.parametrize("coef", ["iso", "general", "per_element", "per_point"])
 @pytest.mark.parametrize("prec", ["fp64", "fp64_fast"])
 def test_diffusion_fp64(ft, O, et, n, rule, coef, prec):
     gen = {"H8": ft.H8block, "H20": ft.H20block, "T4": ft.T4block, "T10": ft.T10block}[et]
@@ -143,9 +143,17 @@ def test_diffusion_fp64(ft, O, et, n, rule, coef, prec):
     elif coef == "general":
         k = np.array([[2.0, 0.3, 0.1], [0.3, 1.5, -0.2], [0.1, -0.2, 1.0]])
         cf, oc, kind = ft.DataCache(k), k, 0
-    else:
+    elif coef == "per_element":
         v = np.random.default_rng(3).lognormal(0, 1, fes.count())
         cf, oc, kind = ft.ElementwiseData(v), v.reshape(-1, 1), 1
+    else:
+        # a DataCache whose fill! varies per element and point, evaluated on
+        # the host at every point (src/DataCacheModule.jl:103-112)
+        npts = femm.integdomain.integrationdata()[0]
+        vals = np.random.default_rng(5).lognormal(0, 1, (fes.count(), npts))
+        cf = ft.DataCache(1.0, lambda cache, XYZ, tangents, feid, qpid:
+                          vals[feid - 1, qpid - 1])
+        oc, kind = vals.reshape(fes.count(), npts, 1), 2
     K = ft.bilform_diffusion(femm, ft.SysmatAssemblerGPU(symmetric=False, precision=prec), geom,
                              u, cf)
     Kr = _oracle_form(O, femm, O.DIFFUSION, geom, u, oc, kind, symmetric=False)
