@@ -857,13 +857,14 @@ int fegpu_bilform_lin_elastic(fegpu_matrix *K, const fegpu_coef *cf, int precisi
           form = F_ELAST_GEN;
           stage_coef(fm, cf, 36, a, st, false);
         }
-      } else if (cf->kind == FEGPU_COEF_PER_ELEMENT && cf->ncomp == 36) {
+      } else if ((cf->kind == FEGPU_COEF_PER_ELEMENT || cf->kind == FEGPU_COEF_PER_QP) &&
+                 cf->ncomp == 36) {
         form = F_ELAST_GEN;
         stage_coef(fm, cf, 36, a, st, false);
       } else {
         throw Error{FEGPU_ERR_ARG,
-                    "lin_elastic: coefficient must be a 6x6 D (constant or per element) or "
-                    "per-element (lambda, mu)"};
+                    "lin_elastic: coefficient must be a 6x6 D (constant, per element or per "
+                    "point) or per-element (lambda, mu)"};
       }
       if (fm->nelem > 0) run_exact(dm, form, a, K->symm_asm);
       else zero_matrix(K);
@@ -890,6 +891,12 @@ int fegpu_bilform_lin_elastic(fegpu_matrix *K, const fegpu_coef *cf, int precisi
     } else if (cf->kind == FEGPU_COEF_PER_ELEMENT && cf->ncomp == 36) {
       form = F_ELAST_GEN;
       stage_coef(fm, cf, 36, a, st, !gather);
+    } else if (cf->kind == FEGPU_COEF_PER_QP) {
+      // these paths apply D to the element's point-summed gradient products,
+      // which needs one D per element
+      throw Error{FEGPU_ERR_ARG,
+                  "lin_elastic: a D that varies over the points of an element needs precision "
+                  "FEGPU_FP64"};
     } else {
       throw Error{FEGPU_ERR_ARG,
                   "lin_elastic: coefficient must be a 6x6 D (constant or per element) or "

@@ -184,7 +184,7 @@ __global__ void __launch_bounds__(kExactThreads) k_blocks_exact(const KArgs a) {
       // ---- DB columns of every node: DB[m][(b,j)] = (Jac w) sum_p D[m][p] B[p][(b,j)]
       for (int i = tid; i < ne * npts * NNE; i += nth) {
         const int eq = i / NNE, b = i - eq * NNE;
-        const int e = eq / npts;
+        const int e = eq / npts, q = eq - e * npts;
         const int64_t es = eb + e;
         const double *gb = sG + (static_cast<size_t>(eq) * NNE + b) * 3;
         const double gx = gb[0], gy = gb[1], gz = gb[2];
@@ -207,7 +207,11 @@ __global__ void __launch_bounds__(kExactThreads) k_blocks_exact(const KArgs a) {
         } else {
           // column (b,x) of B: rows 0 (g_x), 3 (g_y), 4 (g_z); (b,y): 1 (g_y),
           // 3 (g_x), 5 (g_z); (b,z): 2 (g_z), 4 (g_x), 5 (g_y)
-          const double *D = a.coef_kind == FEGPU_COEF_PER_ELEMENT ? a.coef + es * 36 : a.cconst;
+          // D at this point: C = cf(loc, J, i, j) is evaluated at every point
+          // (src/FEMMBaseModule.jl:1802); constant, per element or per point
+          const double *D = a.coef_kind == FEGPU_COEF_PER_ELEMENT ? a.coef + es * 36
+                            : a.coef_kind == FEGPU_COEF_PER_QP   ? a.coef + (es * npts + q) * 36
+                                                                 : a.cconst;
 #pragma unroll
           for (int m = 0; m < 6; ++m) {
             const double *Dm = D + 6 * m;

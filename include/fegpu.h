@@ -167,13 +167,17 @@ int fegpu_matrix_destroy(fegpu_matrix *K);
  * all triples), which decides the last bits of the values. */
 int fegpu_matrix_set_symmetric_assembly(fegpu_matrix *K, int symmetric);
 
-/* The forms.  Each one zeroes K and assembles every element into it with the
- * deterministic colour-ordered scatter.
+/* The forms.  Each one assembles every element into K deterministically:
+ * FEGPU_FP64 by the element-ordered row gather (the reference's own sums,
+ * bit for bit), FEGPU_FP64_FAST by the colour-ordered scatter, FEGPU_MIXED by
+ * the float-float row gather.
  *   bilform_diffusion: src/FEMMBaseModule.jl:1462-1545 (scalar ncomp = 1 ->
  *     _bilform_diffusion_iso, mdim x mdim -> _bilform_diffusion_general);
  *   bilform_lin_elastic(DeforModelRed3D): src/FEMMBaseModule.jl:1774-1824
- *     (ncomp = 36: 6x6 D in Voigt order xx,yy,zz,xy,xz,yz, row-major; or
- *     FEGPU_COEF_ISO_LAME);
+ *     (ncomp = 36: 6x6 D in Voigt order xx,yy,zz,xy,xz,yz, row-major,
+ *     constant, per element, or per point with FEGPU_FP64 only (the other
+ *     precisions apply one D per element to its point-summed gradient
+ *     products); or FEGPU_COEF_ISO_LAME);
  *   bilform_dot: src/FEMMBaseModule.jl:1335-1376 (ncomp = ndn*ndn; m is the
  *     manifold dimension of the measure, as in Jacobianmdim).
  * symmetric = 1 reproduces SysmatAssemblerSparseSymm (the element matrix's

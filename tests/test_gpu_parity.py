@@ -171,7 +171,8 @@ def test_diffusion_fp64(ft, O, et, n, rule, coef, prec):
 # ---------------------------------------------------------------- elasticity
 @pytest.mark.parametrize("et,n,rule", [("H8", 3, ("G", 3, 2)), ("H20", 2, ("G", 3, 3)),
                                        ("T4", 3, ("T", 1)), ("T10", 3, ("T", 4))])
-@pytest.mark.parametrize("coef", ["iso_const", "aniso_const", "per_element_iso", "per_element_D"])
+@pytest.mark.parametrize("coef", ["iso_const", "aniso_const", "per_element_iso", "per_element_D",
+                                  "per_point_D"])
 @pytest.mark.parametrize("prec", ["fp64", "fp64_fast"])
 def test_elasticity_fp64(ft, O, et, n, rule, coef, prec):
     gen = {"H8": ft.H8block, "H20": ft.H20block, "T4": ft.T4block, "T10": ft.T10block}[et]
@@ -197,13 +198,28 @@ def test_elasticity_fp64(ft, O, et, n, rule, coef, prec):
         cf = ft.IsotropicElementwise(E, nu)
         oc = np.stack([ft.isotropic_D(a, b) for a, b in zip(E, nu)]).reshape(-1, 36)
         kind = 1
-    else:
+    elif coef == "per_element_D":
         Ds = []
         for _ in range(fes.count()):
             A = rng.uniform(-1, 1, (6, 6))
             Ds.append(A @ A.T + 6 * np.eye(6))
         oc = np.stack(Ds).reshape(-1, 36)
         cf, kind = ft.ElementwiseData(oc), 1
+    else:
+        # C = cf(loc, J, i, j) varying per point (src/FEMMBaseModule.jl:1802):
+        # an isotropic D whose modulus follows x, evaluated on the host
+        npts = femm.integdomain.integrationdata()[0]
+        def fill(cache, XYZ, tangents, feid, qpid):
+            return ft.isotropic_D(70e9 * (1.0 + XYZ[0, 0]), 0.3)
+        cf = ft.DataCache(ft.isotropic_D(70e9, 0.3), fill)
+        oc = ft.femm._qp_values(femm, geom, cf, 36)
+        kind = 2
+        if prec != "fp64":
+            # the fused paths need one D per element
+            with pytest.raises(ft.FegpuError, match="varies over the points"):
+                ft.bilform_lin_elastic(femm, ft.SysmatAssemblerGPU(precision=prec), geom, u,
+                                       ft.DeforModelRed3D, cf)
+            return
     K = ft.bilform_lin_elastic(femm, ft.SysmatAssemblerGPU(symmetric=False, precision=prec),
                                geom, u, ft.DeforModelRed3D, cf)
     Kr = _oracle_form(O, femm, O.LIN_ELASTIC, geom, u, oc, kind, symmetric=False)
