@@ -799,8 +799,9 @@ int fegpu_bilform_diffusion(fegpu_matrix *K, const fegpu_coef *cf, int precision
       FEGPU_REQUIRE(cf->kind != FEGPU_COEF_ISO_LAME, "diffusion: bad coefficient kind");
     } else {
       FEGPU_REQUIRE(cf->ncomp == md * md, "diffusion: coefficient must be scalar or mdim x mdim");
-      FEGPU_REQUIRE(cf->kind == FEGPU_COEF_CONST || cf->kind == FEGPU_COEF_PER_ELEMENT,
-                    "diffusion: a matrix coefficient must be constant or per element");
+      FEGPU_REQUIRE(cf->kind == FEGPU_COEF_CONST || cf->kind == FEGPU_COEF_PER_ELEMENT ||
+                        cf->kind == FEGPU_COEF_PER_QP,
+                    "diffusion: a matrix coefficient must be constant, per element or per point");
       form = F_DIFF_GEN;
     }
     K->unsym = false;

@@ -254,7 +254,10 @@ __device__ __forceinline__ void qp_weights(const KArgs &a, int64_t es, int q, in
     for (int k = 0; k < NNE * MDIM; ++k) wg[k] = mul(mult, g[k]);
     *jw = mult;
   } else if constexpr (FORM == F_DIFF_GEN) {
-    const double *kap = a.coef_kind == FEGPU_COEF_PER_ELEMENT ? a.coef + es * MDIM * MDIM : a.cconst;
+    // kappa at this point: c = cf(loc, J, i, j) (src/FEMMBaseModule.jl:1497)
+    const double *kap = a.coef_kind == FEGPU_COEF_PER_ELEMENT ? a.coef + es * MDIM * MDIM
+                        : a.coef_kind == FEGPU_COEF_PER_QP   ? a.coef + (es * npts + q) * MDIM * MDIM
+                                                             : a.cconst;
     const T Jw = mul(Jac, T(wq));
 #pragma unroll
     for (int k = 0; k < NNE; ++k)

@@ -290,8 +290,10 @@ __device__ __forceinline__ void mixed_tile(const KArgs &a, int64_t eb, int ne,
       float4 wg = make_float4(w * g[0], w * g[1], w * g[2], 0.f);
       if constexpr (FORM == F_DIFF_GEN) {
         const int e = eq / npts;
-        const double *kap = a.coef_kind == FEGPU_COEF_PER_ELEMENT
-                                ? a.coef + (eb + e) * MDIM * MDIM : a.cconst;
+        const double *kap =
+            a.coef_kind == FEGPU_COEF_PER_ELEMENT ? a.coef + (eb + e) * MDIM * MDIM
+            : a.coef_kind == FEGPU_COEF_PER_QP    ? a.coef + ((eb + e) * npts + q) * MDIM * MDIM
+                                                  : a.cconst;
         float kg[3] = {0.f, 0.f, 0.f};
 #pragma unroll
         for (int m = 0; m < MDIM; ++m)

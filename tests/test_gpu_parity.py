@@ -125,7 +125,8 @@ def _field(ft, n, ndn):
 @pytest.mark.parametrize("et,n,rule", [("H8", 4, ("G", 3, 2)), ("H20", 3, ("G", 3, 3)),
                                        ("T4", 3, ("T", 1)), ("T10", 3, ("T", 4)),
                                        ("H8", 3, ("G", 3, 3)), ("T10", 2, ("T", 5))])
-@pytest.mark.parametrize("coef", ["iso", "general", "per_element", "per_point"])
+@pytest.mark.parametrize("coef", ["iso", "general", "per_element", "per_point",
+                                  "per_point_general"])
 @pytest.mark.parametrize("prec", ["fp64", "fp64_fast"])
 def test_diffusion_fp64(ft, O, et, n, rule, coef, prec):
     gen = {"H8": ft.H8block, "H20": ft.H20block, "T4": ft.T4block, "T10": ft.T10block}[et]
@@ -146,7 +147,7 @@ def test_diffusion_fp64(ft, O, et, n, rule, coef, prec):
     elif coef == "per_element":
         v = np.random.default_rng(3).lognormal(0, 1, fes.count())
         cf, oc, kind = ft.ElementwiseData(v), v.reshape(-1, 1), 1
-    else:
+    elif coef == "per_point":
         # a DataCache whose fill! varies per element and point, evaluated on
         # the host at every point (src/DataCacheModule.jl:103-112)
         npts = femm.integdomain.integrationdata()[0]
@@ -154,6 +155,13 @@ def test_diffusion_fp64(ft, O, et, n, rule, coef, prec):
         cf = ft.DataCache(1.0, lambda cache, XYZ, tangents, feid, qpid:
                           vals[feid - 1, qpid - 1])
         oc, kind = vals.reshape(fes.count(), npts, 1), 2
+    else:
+        # a 3x3 conductivity following the point's coordinates
+        # (_bilform_diffusion_general: c = cf(loc, J, i, j) at every point)
+        k0 = np.array([[2.0, 0.3, 0.1], [0.3, 1.5, -0.2], [0.1, -0.2, 1.0]])
+        cf = ft.DataCache(k0, lambda cache, XYZ, tangents, feid, qpid:
+                          k0 * (1.0 + XYZ[0, 0] + 0.5 * XYZ[0, 2]))
+        oc, kind = ft.femm._qp_values(femm, geom, cf, 9), 2
     K = ft.bilform_diffusion(femm, ft.SysmatAssemblerGPU(symmetric=False, precision=prec), geom,
                              u, cf)
     Kr = _oracle_form(O, femm, O.DIFFUSION, geom, u, oc, kind, symmetric=False)
@@ -162,7 +170,14 @@ def test_diffusion_fp64(ft, O, et, n, rule, coef, prec):
     Ksr = _oracle_form(O, femm, O.DIFFUSION, geom, u, oc, kind)
     if prec == "fp64":
         bitwise(K, Kr)
-        bitwise(ft.bilform_diffusion(femm, geom, u, cf), Ksr)  # the 4-argument form
+        K64 = ft.bilform_diffusion(femm, geom, u, cf)  # the 4-argument form
+        bitwise(K64, Ksr)
+        # the mixed path takes the same point values (rules with positive
+        # weights: the 5-point tetrahedral rule's negative centroid weight
+        # makes every entry a cancellation, 1.1e-6 of the row scale in FP32)
+        if coef.startswith("per_point") and femm.integdomain.integrationdata()[3].min() > 0:
+            mixed_gate(ft.bilform_diffusion(femm, ft.SysmatAssemblerGPU(precision="mixed"),
+                                            geom, u, cf), K64)
     else:
         Ks = ft.bilform_diffusion(femm, ft.SysmatAssemblerGPU(precision=prec), geom, u, cf)
         compare(Ks, Ksr, structure=False)
