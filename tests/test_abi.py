@@ -47,3 +47,22 @@ def test_argument_errors_without_gpu(ft):
     h = ctypes.c_void_p()
     assert L.fegpu_context_create(-1, ctypes.byref(h)) != 0
     assert L.fegpu_assembler_create(None, 1, 3, 3, ctypes.byref(h)) != 0
+
+
+def test_mesh_memory_estimate_without_gpu(ft):
+    """fegpu_estimate_mesh_bytes (the serving loop's admission estimate) is
+    host arithmetic: it grows with the mesh, with the DOFs per node and with
+    the element's node count, rejects unknown element types and negative
+    sizes, and its figure for the T10 60^3 configuration (1,296,000 elements,
+    1,771,561 nodes, 3 DOFs per node, 451,604,169 stored values) covers at
+    least the values (8 bytes each) and the column indices (4 bytes each)."""
+    E60, N60 = 1_296_000, 1_771_561
+    b = ft.estimate_mesh_bytes(4, E60, N60, 3)  # FEGPU_T10
+    assert b >= 451_604_169 * 12
+    assert b < 451_604_169 * 40
+    assert ft.estimate_mesh_bytes(4, 2 * E60, 2 * N60, 3) > b
+    assert ft.estimate_mesh_bytes(4, E60, N60, 1) < b
+    assert ft.estimate_mesh_bytes(2, 64_000, 270_641, 3) > ft.estimate_mesh_bytes(1, 64_000, 68_921, 3)
+    for bad in ((9, 10, 10, 1), (1, -1, 10, 1), (1, 10, 10, 4)):
+        with pytest.raises(ft.FegpuError):
+            ft.estimate_mesh_bytes(*bad)
