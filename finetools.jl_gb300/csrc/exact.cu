@@ -204,8 +204,8 @@ void build_exact_plan(fegpu_dofmap *dm, int block_values, int form) {
 
 }  // namespace
 
-// elements per tile of the reference-order block kernel: the shared memory
-// of two CTAs per SM (one for the largest elements), at least one element
+// elements per tile of the reference-order block kernel: what fits the
+// shared-memory budget of one of its CTAs (below), at least one element
 int exact_tile(int etype, int form, int npts) {
   const int nne = nodes_per_elem(etype), mdim = manif_dim(etype);
   const size_t one = exact_layout(nne, mdim, npts, 1, form).total;
@@ -216,8 +216,9 @@ int exact_tile(int etype, int form, int npts) {
   // shared memory each.  T10 and H20 elasticity, whose point sums run on the
   // integer units, take three CTAs per SM instead (more warps to cover the
   // integer chains' latency): 16 T10 elements per tile (T10 60^3: 30.3
-  // against 31.4 ms with 26 and two CTAs), one H20 element (H20 40^3: 31.2
-  // against 40.0 ms with three and one CTA)
+  // against 31.4 ms with 26 and two CTAs; 14, 15, 17, 18 and 20 per tile
+  // slower), one H20 element (H20 40^3: 31.2 against 40.0 ms with three and
+  // one CTA)
   const bool elast = form == F_ELAST_ISO || form == F_ELAST_GEN;
   size_t budget = per > 24 * 1024 ? 220 * 1024 : 110 * 1024;
   if (elast && etype == FEGPU_T10) budget = 68 * 1024;
