@@ -93,18 +93,37 @@ __device__ __forceinline__ void gather_node_exact(const GArgs &g, int32_t A, dou
   int64_t base[NDN];
 #pragma unroll
   for (int i = 0; i < NDN; ++i) base[i] = g.rowptr[g.dof[A * NDN + i]];
+  // S + S', and (S + S) / 2 on the diagonal.  With three rows per node the
+  // diagonal entries are formed apart by the first three lanes (a select
+  // between the two forms issues all three FP64 operations for every value:
+  // T10 60^3 29.4 -> 29.3 ms, H20 40^3 30.1 -> 29.6 ms); with one row per
+  // node (diffusion) the select stays: H8 20^3 showed no difference beyond
+  // its run-to-run spread.
+  constexpr bool APART = SYM && NDN == 3;
   for (int c = lane; c < cols; c += 32) {
     const int64_t off = g.colperm ? g.colperm[g.cpoff[A] * NDN + c] : c;
 #pragma unroll
     for (int i = 0; i < NDN; ++i) {
       const double l = lo[i * cmax + c];
       double v = l;
-      if (SYM) {
-        // S + S': (S + S) / 2 on the diagonal
+      if (APART) {
+        if (c == self * NDN + i) continue;
+        v = __dadd_rn(l, up[i * cmax + c]);
+      } else if (SYM) {
         v = (c == self * NDN + i) ? __dmul_rn(__dadd_rn(l, l), 0.5) : __dadd_rn(l, up[i * cmax + c]);
       }
       if (dcheck(g.check, CK_GATHER, base[i] + off, g.nnz)) g.val[base[i] + off] = v;
     }
+  }
+  if (APART && lane < NDN) {
+    const int i = lane, c = self * NDN + i;
+    int64_t bi = base[0];  // base[i] without indexing the array by a lane value
+#pragma unroll
+    for (int k = 1; k < NDN; ++k) bi = i == k ? base[k] : bi;
+    const int64_t off = g.colperm ? g.colperm[g.cpoff[A] * NDN + c] : c;
+    const double l = lo[i * cmax + c];
+    const double v = __dmul_rn(__dadd_rn(l, l), 0.5);
+    if (dcheck(g.check, CK_GATHER, bi + off, g.nnz)) g.val[bi + off] = v;
   }
   __syncwarp();
 }
