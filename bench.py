@@ -385,6 +385,14 @@ def fp64_peak_tflops(torch):
     return 2 * 8192 ** 3 / (ms * 1e-3) / 1e12
 
 
+def exact_integer_ops_per_element(nne, npts):
+    """Sums of the reference-order isotropic elasticity blocks that run on the
+    integer units, per element: per point, the nine sums over the points of an
+    off-diagonal node-pair block (six of a diagonal one) and the first sum of
+    each diagonal entry's three products (three)."""
+    return npts * ((nne * (nne - 1) // 2) * (9 + 3) + nne * (6 + 3))
+
+
 def exact_ops_per_element(nne, npts, nnz_per_element, ndn=3):
     """FP64 instructions per element of the reference-order path (isotropic
     D; every one a separately rounded multiply or add): per point J (2 nne 9),
@@ -467,6 +475,7 @@ def run_ours(args):
     traffic = traffic_record().get("t10_exact", {}).get("bytes_per_assembly")
     fp64_peak = fp64_peak_tflops(torch)
     ops = exact_ops_per_element(10, 4, nnz / E) * E
+    int_ops = exact_integer_ops_per_element(10, 4) * E
 
     # ---------------- end to end through the C ABI with host buffers
     # Each step uploads the coordinates from pinned host memory, assembles and
@@ -615,17 +624,21 @@ def run_ours(args):
                                "elements; timed together",
                      "kernel_ms_per_assembly": kernel_ms_step,
                      "note": "bound by the FP64 pipe, not HBM: see fp64_pipe"},
-        "fp64_pipe": {"achieved_instructions_per_s": ops / (kernel_ms_step * 1e-3),
+        "fp64_pipe": {"achieved_instructions_per_s": (ops - int_ops) / (kernel_ms_step * 1e-3),
                       "peak_instructions_per_s": fp64_peak * 1e12 / 2,
-                      "frac": ops / (kernel_ms_step * 1e-3) / (fp64_peak * 1e12 / 2),
+                      "frac": (ops - int_ops) / (kernel_ms_step * 1e-3) / (fp64_peak * 1e12 / 2),
                       "peak_source": "measured: torch.matmul float64 8192^3 (TFLOP/s / 2 = "
                                      "FP64 FMA instructions per second)",
                       "dgemm_tflops": fp64_peak,
-                      "instructions_per_assembly": ops,
-                      "note": "operations of the reference's order, every one a separately "
-                              "rounded FP64 multiply or add; the element blocks' sums over the "
-                              "points run on the integer units (bit-identical IEEE additions), "
-                              "so the rate counts them though the FP64 pipe does not issue them"},
+                      "instructions_per_assembly": ops - int_ops,
+                      "reference_operations_per_assembly": ops,
+                      "reference_operations_per_s": ops / (kernel_ms_step * 1e-3),
+                      "integer_unit_sums_per_assembly": int_ops,
+                      "note": "the reference's order: every operation a separately rounded "
+                              "FP64 multiply or add; the element blocks' sums over the points "
+                              "and the first sum of each diagonal entry run on the integer "
+                              "units (bit-identical IEEE additions), the rest (instructions) "
+                              "on the FP64 pipe"},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "elements/s", "h2d_bytes_per_step": N * 3 * 8,
                 "d2h_bytes_per_step": nnz * 8,
