@@ -225,12 +225,17 @@ void launch_lane(fegpu_server *s, fegpu_server::Lane &R, const std::vector<int64
   std::vector<BatchJob> jobs;
   std::vector<const fegpu_dofmap *> dms;
   for (size_t k = 0; k < ids.size(); ++k) {
+    // the request and its mesh are looked up under the lock: a concurrent
+    // submission or admission may grow the request map or the mesh list
+    // (the objects themselves stay where they are)
     fegpu_server::Request *r;
+    fegpu_server::Mesh *Mp;
     {
       std::lock_guard<std::mutex> lock(s->mu);
       r = &s->requests[ids[k]];
+      Mp = s->meshes[r->mesh].get();
     }
-    fegpu_server::Mesh &M = *s->meshes[r->mesh];
+    fegpu_server::Mesh &M = *Mp;
     fegpu_femm *fm = M.K->dm->femm;
     if (starts[k]) {
       if (r->kind == FEGPU_REQUEST_COEF) {
@@ -275,11 +280,13 @@ void launch_lane(fegpu_server *s, fegpu_server::Lane &R, const std::vector<int64
 // One FP64 request through the single-call form (worker thread, no lock held).
 void run_fp64(fegpu_server *s, int64_t id) {
   fegpu_server::Request *r;
+  fegpu_server::Mesh *Mp;
   {
     std::lock_guard<std::mutex> lock(s->mu);
     r = &s->requests[id];
+    Mp = s->meshes[r->mesh].get();
   }
-  fegpu_server::Mesh &M = *s->meshes[r->mesh];
+  fegpu_server::Mesh &M = *Mp;
   fegpu_femm *fm = M.K->dm->femm;
   fegpu_coef cf = M.cf;
   if (r->kind == FEGPU_REQUEST_COEF) {
